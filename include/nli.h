@@ -1,0 +1,264 @@
+/*
+ * nli.h -- C ABI of the GB300 (sm_103a) multiscale non-local inpainting path.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, and
+ * returns an int status (NLI_OK == 0).  Unless a function says "host
+ * pointers", every array argument is a CUDA device pointer on the context's
+ * device, and all work is enqueued on the context's stream.  Functions that
+ * return a scalar result (an energy, a total difference) synchronise that
+ * stream before returning.
+ *
+ * Data layout (identical to the reference containers):
+ *   image  : float32, interleaved HWC, element (x, y, c) at C*(W*y + x) + c
+ *            (image.hpp:481-485, FixedImage<T>::get_index)
+ *   mask   : uint8 per pixel, 0 or 1 (FixedMask stores one bool per pixel)
+ *   NNF    : int32 pairs, element (x, y) at 2*(W*y + x): the absolute centre
+ *            (x, y) of the matched source patch, (-1, -1) for none
+ *            (Image<Point>, patch_match.cpp:335)
+ *   gradient: float32, 2C interleaved channels [gx_0, gy_0, gx_1, gy_1, ...]
+ *            (gradient.cpp:36-70)
+ *
+ * Each declaration names the reference interface it replaces (file:line in
+ * Tom-Zheng/non-local-inpainting).
+ */
+#ifndef NLI_H_
+#define NLI_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+enum {
+	NLI_OK = 0,
+	NLI_E_INVALID = -1,          /* bad argument (null pointer, size <= 0, ...) */
+	NLI_E_EMPTY_SOURCE = -2,     /* image_inpainting.cpp:382-384 "Empty source mask" */
+	NLI_E_CHANNELS = -3,         /* l2_rgbd_patch_distance.cpp:112 "Channels do not match" */
+	NLI_E_SHAPE = -4,            /* size mismatch; PatchMatch::calculate returns an empty
+	                                image in this case (patch_match.cpp:317-322) */
+	NLI_E_UNSUPPORTED = -5,      /* distance / updater / patch size with no GPU kernel */
+	NLI_E_CUDA = -6,             /* a CUDA runtime call failed */
+	NLI_E_TIMEOUT = -7,          /* a device-side wait ran out of its iteration budget */
+	NLI_E_NOMEM = -8             /* device allocation failed */
+};
+
+/* APatchDistance subclasses (a_patch_distance.h:24) */
+enum {
+	NLI_DIST_L2_COMBINED = 0,    /* L2CombinedPatchDistance (l2_combined_patch_distance.cpp:39-148) */
+	NLI_DIST_L2_RGBD = 1,        /* L2RGBDPatchDistance (l2_rgbd_patch_distance.cpp:41-117) */
+	NLI_DIST_L2_NORM = 2,        /* L2NormPatchDistance (l2_norm_patch_distance.cpp:22-104) */
+	NLI_DIST_L1_NORM = 3         /* L1NormPatchDistance (l1_norm_patch_distance.cpp:22-105) */
+};
+
+/* AImageUpdating subclasses (a_image_updating.h:27) */
+enum {
+	NLI_UPDATE_MEANS = 0,        /* PatchNonLocalMeans   (patch_non_local_means.cpp:23-100) */
+	NLI_UPDATE_MEDIANS = 1,      /* PatchNonLocalMedians (patch_non_local_medians.cpp:23-127) */
+	NLI_UPDATE_POISSON = 2,      /* PatchNonLocalPoisson (patch_non_local_poisson.cpp:36-477) */
+	NLI_UPDATE_DEPTH = 3         /* PatchNonLocalDepth   (patch_non_local_depth.cpp:36-55) */
+};
+
+/* ImageInpainting::InitType, same order (image_inpainting.h:41) */
+enum {
+	NLI_INIT_BLACK = 0,
+	NLI_INIT_AVG = 1,
+	NLI_INIT_NONE = 2,
+	NLI_INIT_POISSON = 3
+};
+
+#define NLI_MAX_PATCH 15      /* largest patch side with a GPU kernel */
+#define NLI_MAX_SCALES 32
+
+/* Parameters of an APatchDistance object (a_patch_distance.h:28,
+ * l2_combined_patch_distance.h:31, l2_rgbd_patch_distance.h:31). */
+typedef struct nli_distance_params {
+	int32_t kind;        /* NLI_DIST_* */
+	int32_t patch_x;     /* Shape::size_x of the patch */
+	int32_t patch_y;     /* Shape::size_y of the patch */
+	float   sigma;       /* Gaussian sigma of the intra-patch weights */
+	float   lambda;      /* L2Combined: lambda.  L2RGBD: lambda_rgb */
+	float   lambda_d;    /* L2RGBD: lambda of the depth channel */
+} nli_distance_params;
+
+/* Parameters of a PatchMatch object (patch_match.h:44-47). */
+typedef struct nli_patchmatch_params {
+	int32_t iterations;    /* sweeps per calculate() (reference default 10) */
+	int32_t random_shots;  /* shots per random-search window (CLI: 30) */
+	int32_t window;        /* largest random-search window; -1 = max(W, H) */
+} nli_patchmatch_params;
+
+/* Parameters of an AImageUpdating object (a_image_updating.h:28,
+ * patch_non_local_poisson.h:29-33, patch_non_local_depth.h). */
+typedef struct nli_update_params {
+	int32_t method;      /* NLI_UPDATE_* */
+	int32_t patch_x;
+	int32_t patch_y;
+	float   sigma;       /* Gaussian sigma of the patch weights */
+	float   lambda;      /* NL-Poisson: lambda.  NL-depth: lambda_rgb */
+	float   lambda_d;    /* NL-depth: lambda of the depth channel */
+	float   cg_tol;      /* CG stops when |r|^2 < cg_tol * |r0|^2 */
+	int32_t cg_iters;    /* CG iteration limit */
+} nli_update_params;
+
+/* Parameters of an ImageInpainting object (image_inpainting.h:44-50) plus
+ * the objects it is wired to (main.cpp:236-270). */
+typedef struct nli_process_params {
+	nli_distance_params   distance;
+	nli_patchmatch_params patchmatch;
+	nli_update_params     update;
+	int32_t iterations;         /* iterations_amount */
+	float   tolerance;          /* stop a scale when sum (du)^2 <= tolerance */
+	int32_t scales;             /* scales_amount */
+	float   subsampling_rate;   /* see nli_subsampling_rate() */
+	float   conf_decay_time;    /* confidence_decay_time */
+	float   conf_asymptotic;    /* confidence_asymptotic_value */
+	int32_t init;               /* NLI_INIT_* */
+} nli_process_params;
+
+/* What one process() call did (the reference prints these, image_inpainting.cpp:165-407). */
+typedef struct nli_process_stats {
+	int32_t scales;
+	int32_t width[NLI_MAX_SCALES];       /* index 0 = finest */
+	int32_t height[NLI_MAX_SCALES];
+	int32_t iterations[NLI_MAX_SCALES];  /* inpaint_internal iterations per scale */
+	double  last_difference[NLI_MAX_SCALES];
+	int64_t patchmatch_calls;
+	int64_t update_calls;
+	int64_t cg_iterations;               /* summed over channels and solves */
+	int64_t candidates;                  /* patch distances evaluated by PatchMatch */
+} nli_process_stats;
+
+typedef struct nli_ctx nli_ctx;
+
+/* ---- context ------------------------------------------------------------- */
+const char *nli_version(void);
+const char *nli_status_string(int status);
+/* Creates a context on CUDA device `device` with its own non-blocking stream. */
+int nli_ctx_create(int device, nli_ctx **out);
+int nli_ctx_destroy(nli_ctx *ctx);
+/* Enqueues all further work of this context on `stream` (a cudaStream_t;
+ * NULL is the legacy default stream) instead of the context's own
+ * non-blocking stream. */
+int nli_ctx_set_stream(nli_ctx *ctx, void *stream);
+/* Seed of the counter-based PatchMatch RNG.  The reference seeds rand() with
+ * srand(time(NULL)) (main.cpp:273); a fixed seed makes runs repeatable. */
+int nli_set_seed(nli_ctx *ctx, uint64_t seed);
+int nli_ctx_synchronize(nli_ctx *ctx);
+/* Message of the last failing call on this context (never NULL). */
+const char *nli_last_error(nli_ctx *ctx);
+
+/* ---- numeric helpers (L1) ------------------------------------------------ */
+/* GaussianWeights::calculate (gaussian_weights.cpp:19-79).  Host pointers:
+ * writes size_x*size_y floats.  size_y == 1 gives the 1-D form used by the
+ * pyramid filter (exp(-x^2/sigma^2), gaussian_weights.cpp:37). */
+int nli_gaussian_weights(int size_x, int size_y, float sigma_x, float sigma_y, float *host_out);
+
+/* ImageInpainting::calculate_subsampling_rate (image_inpainting.cpp:197-204). */
+float nli_subsampling_rate(float size_ratio, unsigned int scales);
+
+/* Sampling::_Details::get_sample_size (sampling.cpp:408-411). */
+int nli_sample_size(int size, float factor);
+
+/* Gradient::calculate, forward differences (gradient.cpp:20-75). */
+int nli_gradient(nli_ctx *ctx, const float *image, int W, int H, int C, float *gradient);
+
+/* Sampling::downsample_with_mask (sampling.cpp:114-202).  out_image must hold
+ * oW*oH*C floats and out_mask oW*oH bytes, oW = nli_sample_size(W, factor). */
+int nli_downsample_with_mask(nli_ctx *ctx, const float *image, const uint8_t *mask,
+                             int W, int H, int C, float factor, float threshold, int mask_val,
+                             float *out_image, uint8_t *out_mask);
+
+/* Sampling::upsample, nearest neighbour (sampling.cpp:205-246, 387-406). */
+int nli_upsample(nli_ctx *ctx, const float *image, int W, int H, int C,
+                 int out_W, int out_H, float *out_image);
+
+/* DistanceTransform::calculate (distance_transform.cpp:20-99): distance of
+ * every pixel to the nearest pixel with mask == 0. */
+int nli_distance_transform(nli_ctx *ctx, const uint8_t *mask, int W, int H, float *distances);
+
+/* ImageInpainting::calculate_confidence_mask (image_inpainting.cpp:611-630). */
+int nli_confidence_mask(nli_ctx *ctx, const uint8_t *mask, int W, int H,
+                        float decay_time, float asymptotic_value, float *confidence);
+
+/* ImageInpainting::get_extended_domain (image_inpainting.cpp:566-600). */
+int nli_extended_domain(nli_ctx *ctx, const uint8_t *mask, int W, int H,
+                        int patch_x, int patch_y, uint8_t *extended);
+
+/* Source and target masks of one scale: target = extended domain, source =
+ * its complement, eroded where the right or bottom neighbour is not source
+ * when `erode` != 0 (image_inpainting.cpp:361-377), then a `margin` wide
+ * border is cleared in both (add_margin, image_inpainting.cpp:641-657).
+ * *source_empty is set as image_inpainting.cpp:368-384 computes it (before
+ * the margin).  With erode == 0 this is the mask pair of propagate_weights
+ * (image_inpainting.cpp:501-506, 545-549). */
+int nli_scale_masks(nli_ctx *ctx, const uint8_t *extended, int W, int H, int margin, int erode,
+                    uint8_t *source, uint8_t *target, int *source_empty);
+
+/* Coarsest-scale hole filling, InitPoisson branch of ImageInpainting::process
+ * (image_inpainting.cpp:125-153) -> poisson_solver_separable_simplest
+ * (3rdparty/simpois/simpois.c:281-291).  Replaces image pixels where mask != 0. */
+int nli_poisson_init(nli_ctx *ctx, float *image, const uint8_t *mask, int W, int H, int C);
+
+/* ---- patch distances (L2a) ----------------------------------------------- */
+/* APatchDistance::calculate over a list of pairs (a_patch_distance.h:34,
+ * l2_combined_patch_distance.cpp:39-148, l2_rgbd_patch_distance.cpp:41-117,
+ * l2_norm_patch_distance.cpp:22-104, l1_norm_patch_distance.cpp:22-105).
+ * pairs: n x int32[4] = (source x, source y, target x, target y), patch
+ * centres; every patch must lie inside its image.  Source and target are
+ * initialize()d from `source` and `target` (gradients computed here).
+ * Arithmetic follows the reference: per-tap float norms, double sums. */
+int nli_distance_pairs(nli_ctx *ctx, const nli_distance_params *dist,
+                       const float *source, int sW, int sH,
+                       const float *target, int tW, int tH, int C,
+                       const int32_t *pairs, int n, float *out);
+
+/* Exhaustive nearest neighbour: for every target pixel with target_mask != 0,
+ * the source pixel with source_mask != 0 of least distance (ties -> lowest
+ * raster index y*sW + x).  Same arithmetic as nli_distance_pairs.  Points
+ * whose patch would leave its image are skipped (NNF (-1,-1)). */
+int nli_bruteforce_nnf(nli_ctx *ctx, const nli_distance_params *dist,
+                       const float *source, const uint8_t *source_mask, int sW, int sH,
+                       const float *target, const uint8_t *target_mask, int tW, int tH, int C,
+                       int32_t *nnf, float *distance);
+
+/* ---- correspondence (L3) ------------------------------------------------- */
+/* PatchMatch::calculate (patch_match.cpp:311-512).  init_nnf may be NULL
+ * (random initialisation, patch_match.cpp:361-381).  out_nnf gets tW*tH
+ * pairs, (-1,-1) outside target_mask; out_distance (may be NULL) gets the
+ * matched distance (FLT_MAX where none); *energy (may be NULL) gets the sum
+ * of matched distances over the target points. */
+int nli_patchmatch(nli_ctx *ctx, const nli_distance_params *dist, const nli_patchmatch_params *pm,
+                   const float *source, const uint8_t *source_mask, int sW, int sH,
+                   const float *target, const uint8_t *target_mask, int tW, int tH, int C,
+                   const int32_t *init_nnf, int32_t *out_nnf, float *out_distance, double *energy);
+
+/* ---- image updating (L2b) ------------------------------------------------ */
+/* AImageUpdating::update (a_image_updating.h:34-39): updates `image` in
+ * place on `domain`, returns sum over domain of (old - new)^2.  `orig` may
+ * alias `image`.  confidence may be NULL (all ones). */
+int nli_update(nli_ctx *ctx, const nli_update_params *upd,
+               float *image, const float *orig, const uint8_t *domain, const uint8_t *ext_domain,
+               const int32_t *nnf, const float *confidence, int W, int H, int C,
+               double *total_difference);
+
+/* ---- multiscale driver (L4) ---------------------------------------------- */
+/* ImageInpainting::process (image_inpainting.cpp:68-190).  Host pointers:
+ * image (W*H*C floats), mask (W*H bytes), out (W*H*C floats).  The host
+ * copies are part of the call.  stats may be NULL. */
+int nli_process(nli_ctx *ctx, const nli_process_params *params,
+                const float *image, const uint8_t *mask, int W, int H, int C,
+                float *out, nli_process_stats *stats);
+
+/* Same as nli_process with device pointers (no host copies). */
+int nli_process_device(nli_ctx *ctx, const nli_process_params *params,
+                       const float *image, const uint8_t *mask, int W, int H, int C,
+                       float *out, nli_process_stats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NLI_H_ */

@@ -1,0 +1,312 @@
+"""GB300-native (sm_103a) multiscale non-local inpainting.
+
+Python front end of the C ABI in include/nli.h (libnli_gb300.so, built
+in-tree by build.py).  Device arrays are torch CUDA tensors; the multiscale
+`process` also accepts host numpy arrays (the host copies are then part of
+the call, as in nli_process).  There is no CPU implementation here: every
+call runs CUDA kernels, and loading fails loudly when the library is
+missing.
+"""
+from __future__ import annotations
+
+import ctypes as ct
+import os
+
+import numpy as np
+
+from . import _abi
+from ._abi import (DistanceParams, PatchMatchParams, ProcessParams, ProcessStats,  # noqa: F401
+                   UpdateParams)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libnli_gb300.so")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "nli.h")
+
+_lib = None
+
+P = ct.c_void_p
+I = ct.c_int
+F = ct.c_float
+
+
+class NliError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s (%d): %s" % (_abi_status(status), status, message))
+        self.status = status
+
+
+def _abi_status(s):
+    names = {0: "ok", -1: "invalid argument", -2: "empty source mask", -3: "channels do not match",
+             -4: "size mismatch", -5: "unsupported", -6: "CUDA error", -7: "timeout", -8: "out of memory"}
+    return names.get(s, "status")
+
+
+def exported_symbols():
+    """Names of the functions declared in include/nli.h."""
+    import re
+    txt = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(nli_[a-z_0-9]+)\s*\(", txt, re.M)))
+
+
+def load(path=LIB_PATH):
+    """Loads libnli_gb300.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError("libnli_gb300.so not found at %s: run __graft_entry__.build()" % path)
+    L = ct.CDLL(path)
+
+    def proto(name, res, args):
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+
+    dp, pp, up, prp, st = (ct.POINTER(DistanceParams), ct.POINTER(PatchMatchParams), ct.POINTER(UpdateParams),
+                           ct.POINTER(ProcessParams), ct.POINTER(ProcessStats))
+    proto("nli_version", ct.c_char_p, [])
+    proto("nli_status_string", ct.c_char_p, [I])
+    proto("nli_ctx_create", I, [I, ct.POINTER(P)])
+    proto("nli_ctx_destroy", I, [P])
+    proto("nli_ctx_set_stream", I, [P, P])
+    proto("nli_set_seed", I, [P, ct.c_uint64])
+    proto("nli_ctx_synchronize", I, [P])
+    proto("nli_last_error", ct.c_char_p, [P])
+    proto("nli_gaussian_weights", I, [I, I, F, F, P])
+    proto("nli_subsampling_rate", F, [F, ct.c_uint])
+    proto("nli_sample_size", I, [I, F])
+    proto("nli_gradient", I, [P, P, I, I, I, P])
+    proto("nli_downsample_with_mask", I, [P, P, P, I, I, I, F, F, I, P, P])
+    proto("nli_upsample", I, [P, P, I, I, I, I, I, P])
+    proto("nli_distance_transform", I, [P, P, I, I, P])
+    proto("nli_confidence_mask", I, [P, P, I, I, F, F, P])
+    proto("nli_extended_domain", I, [P, P, I, I, I, I, P])
+    proto("nli_scale_masks", I, [P, P, I, I, I, I, P, P, ct.POINTER(I)])
+    proto("nli_poisson_init", I, [P, P, P, I, I, I])
+    proto("nli_distance_pairs", I, [P, dp, P, I, I, P, I, I, I, P, I, P])
+    proto("nli_bruteforce_nnf", I, [P, dp, P, P, I, I, P, P, I, I, I, P, P])
+    proto("nli_patchmatch", I, [P, dp, pp, P, P, I, I, P, P, I, I, I, P, P, P, ct.POINTER(ct.c_double)])
+    proto("nli_update", I, [P, up, P, P, P, P, P, P, I, I, I, ct.POINTER(ct.c_double)])
+    proto("nli_process", I, [P, prp, P, P, I, I, I, P, st])
+    proto("nli_process_device", I, [P, prp, P, P, I, I, I, P, st])
+    _lib = L
+    return L
+
+
+def _ptr(t):
+    """Device pointer of a torch tensor (None passes NULL)."""
+    if t is None:
+        return None
+    return ct.c_void_p(t.data_ptr())
+
+
+def _dims(t):
+    if t.dim() == 2:
+        return t.shape[1], t.shape[0], 1
+    return t.shape[1], t.shape[0], t.shape[2]
+
+
+class Context:
+    """One nli_ctx: a CUDA device, a stream, the PatchMatch seed and the
+    device workspace.  Not thread-safe (one per host thread)."""
+
+    def __init__(self, device=0):
+        import torch
+        self.torch = torch
+        self.lib = load()
+        self.device = device
+        torch.cuda.init()
+        h = ct.c_void_p()
+        self.h = None
+        self._check(self.lib.nli_ctx_create(device, ct.byref(h)), ctx=None)
+        self.h = h
+        # order the library's kernels with torch's own work on this device
+        self.set_stream(torch.cuda.current_stream(device))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.nli_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, ctx="self"):
+        if rc != 0:
+            msg = self.lib.nli_last_error(self.h).decode() if ctx is not None and self.h else ""
+            raise NliError(rc, msg)
+
+    def set_seed(self, seed):
+        self._check(self.lib.nli_set_seed(self.h, seed))
+
+    def set_stream(self, stream):
+        """Runs subsequent calls on a torch.cuda.Stream."""
+        self._check(self.lib.nli_ctx_set_stream(self.h, ct.c_void_p(stream.cuda_stream)))
+
+    def synchronize(self):
+        self._check(self.lib.nli_ctx_synchronize(self.h))
+
+    # -- device tensors helpers
+    def _f32(self, a):
+        t = self.torch
+        if isinstance(a, np.ndarray):
+            a = t.from_numpy(np.ascontiguousarray(a, np.float32))
+        return a.to(device="cuda:%d" % self.device, dtype=t.float32).contiguous()
+
+    def _u8(self, a):
+        t = self.torch
+        if isinstance(a, np.ndarray):
+            a = t.from_numpy(np.ascontiguousarray(a).astype(np.uint8))
+        return a.to(device="cuda:%d" % self.device, dtype=t.uint8).contiguous()
+
+    def _i32(self, a):
+        t = self.torch
+        if isinstance(a, np.ndarray):
+            a = t.from_numpy(np.ascontiguousarray(a, np.int32))
+        return a.to(device="cuda:%d" % self.device, dtype=t.int32).contiguous()
+
+    def _empty(self, shape, dtype):
+        return self.torch.empty(shape, dtype=dtype, device="cuda:%d" % self.device)
+
+    # -- L1 helpers
+    def gradient(self, img):
+        img = self._f32(img)
+        W, H, C = _dims(img)
+        out = self._empty((H, W, 2 * C), self.torch.float32)
+        self._check(self.lib.nli_gradient(self.h, _ptr(img), W, H, C, _ptr(out)))
+        return out
+
+    def gaussian_weights(self, sx, sy, sigma_x, sigma_y):
+        out = np.empty((sy, sx), np.float32)
+        rc = self.lib.nli_gaussian_weights(sx, sy, sigma_x, sigma_y, out.ctypes.data_as(P))
+        if rc:
+            raise NliError(rc, "gaussian_weights")
+        return out
+
+    def sample_size(self, size, factor):
+        return self.lib.nli_sample_size(size, factor)
+
+    def downsample_with_mask(self, img, mask, factor, threshold=0.4, mask_val=False):
+        img, mask = self._f32(img), self._u8(mask)
+        W, H, C = _dims(img)
+        sW, sH = self.sample_size(W, factor), self.sample_size(H, factor)
+        oi = self._empty((sH, sW, C), self.torch.float32)
+        om = self._empty((sH, sW), self.torch.uint8)
+        self._check(self.lib.nli_downsample_with_mask(self.h, _ptr(img), _ptr(mask), W, H, C, factor, threshold,
+                                                      1 if mask_val else 0, _ptr(oi), _ptr(om)))
+        return oi, om
+
+    def upsample(self, img, oW, oH):
+        img = self._f32(img)
+        W, H, C = _dims(img)
+        out = self._empty((oH, oW, C), self.torch.float32)
+        self._check(self.lib.nli_upsample(self.h, _ptr(img), W, H, C, oW, oH, _ptr(out)))
+        return out
+
+    def distance_transform(self, mask):
+        mask = self._u8(mask)
+        out = self._empty(tuple(mask.shape), self.torch.float32)
+        self._check(self.lib.nli_distance_transform(self.h, _ptr(mask), mask.shape[1], mask.shape[0], _ptr(out)))
+        return out
+
+    def confidence_mask(self, mask, decay=5.0, asym=0.1):
+        mask = self._u8(mask)
+        out = self._empty(tuple(mask.shape), self.torch.float32)
+        self._check(self.lib.nli_confidence_mask(self.h, _ptr(mask), mask.shape[1], mask.shape[0], decay, asym,
+                                                 _ptr(out)))
+        return out
+
+    def extended_domain(self, mask, px=9, py=9):
+        mask = self._u8(mask)
+        out = self._empty(tuple(mask.shape), self.torch.uint8)
+        self._check(self.lib.nli_extended_domain(self.h, _ptr(mask), mask.shape[1], mask.shape[0], px, py, _ptr(out)))
+        return out
+
+    def scale_masks(self, ext, margin, erode):
+        ext = self._u8(ext)
+        s = self._empty(tuple(ext.shape), self.torch.uint8)
+        t = self._empty(tuple(ext.shape), self.torch.uint8)
+        e = I()
+        self._check(self.lib.nli_scale_masks(self.h, _ptr(ext), ext.shape[1], ext.shape[0], margin, 1 if erode else 0,
+                                             _ptr(s), _ptr(t), ct.byref(e)))
+        return s, t, bool(e.value)
+
+    def poisson_init(self, img, mask):
+        img = self._f32(img).clone()
+        mask = self._u8(mask)
+        W, H, C = _dims(img)
+        self._check(self.lib.nli_poisson_init(self.h, _ptr(img), _ptr(mask), W, H, C))
+        return img
+
+    # -- L2a / L3
+    def distance_pairs(self, dist, src, tgt, pairs):
+        src, tgt, pairs = self._f32(src), self._f32(tgt), self._i32(pairs)
+        sW, sH, C = _dims(src)
+        tW, tH, _ = _dims(tgt)
+        out = self._empty((pairs.shape[0],), self.torch.float32)
+        self._check(self.lib.nli_distance_pairs(self.h, ct.byref(dist), _ptr(src), sW, sH, _ptr(tgt), tW, tH, C,
+                                                _ptr(pairs), pairs.shape[0], _ptr(out)))
+        return out
+
+    def bruteforce_nnf(self, dist, src, smask, tgt, tmask):
+        src, tgt, smask, tmask = self._f32(src), self._f32(tgt), self._u8(smask), self._u8(tmask)
+        sW, sH, C = _dims(src)
+        tW, tH, _ = _dims(tgt)
+        nnf = self._empty((tH, tW, 2), self.torch.int32)
+        d = self._empty((tH, tW), self.torch.float32)
+        self._check(self.lib.nli_bruteforce_nnf(self.h, ct.byref(dist), _ptr(src), _ptr(smask), sW, sH, _ptr(tgt),
+                                                _ptr(tmask), tW, tH, C, _ptr(nnf), _ptr(d)))
+        return nnf, d
+
+    def patchmatch(self, dist, pm, src, smask, tgt, tmask, init=None, want_energy=True):
+        src, tgt, smask, tmask = self._f32(src), self._f32(tgt), self._u8(smask), self._u8(tmask)
+        init = None if init is None else self._i32(init)
+        sW, sH, C = _dims(src)
+        tW, tH, _ = _dims(tgt)
+        nnf = self._empty((tH, tW, 2), self.torch.int32)
+        d = self._empty((tH, tW), self.torch.float32)
+        e = ct.c_double()
+        self._check(self.lib.nli_patchmatch(self.h, ct.byref(dist), ct.byref(pm), _ptr(src), _ptr(smask), sW, sH,
+                                            _ptr(tgt), _ptr(tmask), tW, tH, C, _ptr(init), _ptr(nnf), _ptr(d),
+                                            ct.byref(e) if want_energy else None))
+        return nnf, d, e.value
+
+    # -- L2b
+    def update(self, upd, image, orig, dom, ext, nnf, conf=None, same_orig=False):
+        """Returns (updated image, total difference); `image` is not modified."""
+        img = self._f32(image).clone()
+        W, H, C = _dims(img)
+        org = img if same_orig else self._f32(orig)
+        dom, ext, nnf = self._u8(dom), self._u8(ext), self._i32(nnf)
+        conf = None if conf is None else self._f32(conf)
+        tot = ct.c_double()
+        self._check(self.lib.nli_update(self.h, ct.byref(upd), _ptr(img), _ptr(org), _ptr(dom), _ptr(ext), _ptr(nnf),
+                                        _ptr(conf), W, H, C, ct.byref(tot)))
+        return img, tot.value
+
+    # -- L4
+    def process(self, img, mask, params, stats=True):
+        """ImageInpainting::process on host arrays (numpy in, numpy out)."""
+        img = np.ascontiguousarray(img, np.float32)
+        mask = np.ascontiguousarray(mask).astype(np.uint8)
+        H, W = img.shape[:2]
+        C = 1 if img.ndim == 2 else img.shape[2]
+        out = np.empty_like(img)
+        st = ProcessStats()
+        self._check(self.lib.nli_process(self.h, ct.byref(params), img.ctypes.data_as(P), mask.ctypes.data_as(P),
+                                         W, H, C, out.ctypes.data_as(P), ct.byref(st)))
+        return out, st.as_dict()
+
+    def process_device(self, img, mask, params, out=None):
+        """ImageInpainting::process on device tensors; returns (out, stats)."""
+        img, mask = self._f32(img), self._u8(mask)
+        W, H, C = _dims(img)
+        if out is None:
+            out = self.torch.empty_like(img)
+        st = ProcessStats()
+        self._check(self.lib.nli_process_device(self.h, ct.byref(params), _ptr(img), _ptr(mask), W, H, C, _ptr(out),
+                                                ct.byref(st)))
+        return out, st.as_dict()

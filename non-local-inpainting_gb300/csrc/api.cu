@@ -1,0 +1,361 @@
+// The C ABI (include/nli.h): argument checking, context management and the
+// translation of internal errors into status codes.  Every entry point that
+// computes enqueues CUDA kernels; nothing here falls back to the CPU.
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "nli_device.cuh"
+#include "nli_internal.cuh"
+
+namespace nli {
+
+// GaussianWeights::calculate (gaussian_weights.cpp:19-79, SEGMENTS == 1):
+// pixel-centre samples of exp(-(x^2/(2 sx^2) + y^2/(2 sy^2))) in double
+// (1-D: exp(-x^2/sx^2)), mirrored from the top-left quarter, normalised by
+// their float sum.  Computed once per object on the host, like the
+// reference, and handed to the kernels as a table.
+std::vector<float> gaussian_weights_host(unsigned sx, unsigned sy, float sigma_x, float sigma_y)
+{
+	std::vector<float> w((size_t)sx * sy, 0.0f);
+	const double x_a = -(float)sx / 2, y_a = -(float)sy / 2;
+	if (sy == 1) {
+		for (unsigned i = 0; i <= sx / 2; i++) {
+			double x = x_a + i + 0.5;
+			double value = 0.0;
+			value += exp(-(pow(x, 2) / pow(sigma_x, 2)));
+			w[i] = value;
+		}
+	} else {
+		for (unsigned i = 0; i <= sx / 2; i++)
+			for (unsigned j = 0; j <= sy / 2; j++) {
+				double x = x_a + i + 0.5, y = y_a + j + 0.5;
+				double value = 0.0;
+				value += exp(-(pow(x, 2) / (2 * pow(sigma_x, 2)) + pow(y, 2) / (2 * pow(sigma_y, 2))));
+				w[(size_t)sx * j + i] = value;
+			}
+	}
+	for (unsigned i = 0; i <= sx / 2; i++)
+		for (unsigned j = 0; j <= sy / 2; j++) {
+			float v = w[(size_t)sx * j + i];
+			w[(size_t)sx * j + (sx - 1 - i)] = v;
+			if (sy > 1) {
+				w[(size_t)sx * (sy - 1 - j) + i] = v;
+				w[(size_t)sx * (sy - 1 - j) + (sx - 1 - i)] = v;
+			}
+		}
+	float sum = 0.0f;
+	for (float v : w) sum += v;
+	for (float &v : w) v /= sum;
+	return w;
+}
+
+int feature_float4s(int kind, int C)
+{
+	int comps = (kind == NLI_DIST_L2_COMBINED || kind == NLI_DIST_L2_RGBD) ? 3 * C : C;
+	return (comps + 3) / 4;
+}
+
+void fill_dist_args(DistArgs &a, const nli_distance_params &p, int C)
+{
+	NLI_REQUIRE(p.patch_x >= 1 && p.patch_y >= 1 && p.patch_x <= NLI_MAX_PATCH && p.patch_y <= NLI_MAX_PATCH,
+	            NLI_E_UNSUPPORTED, "patch size outside 1.." + std::to_string(NLI_MAX_PATCH));
+	NLI_REQUIRE(p.kind >= 0 && p.kind <= 3, NLI_E_UNSUPPORTED, "unknown distance kind");
+	NLI_REQUIRE(C >= 1 && C <= 4, NLI_E_UNSUPPORTED, "images must have 1 to 4 channels");
+	if (p.kind == NLI_DIST_L2_RGBD)
+		NLI_REQUIRE(C == 4, NLI_E_CHANNELS, "L2 RGBD Distance: Channels do not match.");
+	std::memset(&a, 0, sizeof(a));
+	a.kind = p.kind;
+	a.px = p.patch_x;
+	a.py = p.patch_y;
+	a.rx = p.patch_x / 2;
+	a.ry = p.patch_y / 2;
+	a.C = C;
+	a.nf4 = feature_float4s(p.kind, C);
+	a.lambda = p.lambda;
+	a.lambda_d = p.lambda_d;
+	std::vector<float> w = gaussian_weights_host(p.patch_x, p.patch_y, p.sigma, p.sigma);
+	std::memcpy(a.weights, w.data(), sizeof(float) * w.size());
+}
+
+}  // namespace nli
+
+using namespace nli;
+
+static int fail(nli_ctx *ctx, const Error &e)
+{
+	if (ctx) ctx->last_error = e.message;
+	return e.status;
+}
+
+#define API_BEGIN(ctx)                                                   \
+	if (!(ctx)) return NLI_E_INVALID;                                    \
+	try {                                                                \
+		NLI_CUDA(cudaSetDevice((ctx)->device));
+
+#define API_END(ctx)                                                     \
+	}                                                                    \
+	catch (const Error &e) {                                             \
+		return fail(ctx, e);                                             \
+	}                                                                    \
+	catch (const std::bad_alloc &) {                                     \
+		return fail(ctx, Error{NLI_E_NOMEM, "host allocation failed"}); \
+	}                                                                    \
+	return NLI_OK;
+
+static void require_ptrs(std::initializer_list<const void *> ps)
+{
+	for (const void *p : ps) NLI_REQUIRE(p != nullptr, NLI_E_INVALID, "null pointer argument");
+}
+
+static void require_dims(int W, int H, int C)
+{
+	NLI_REQUIRE(W > 0 && H > 0, NLI_E_INVALID, "image sizes must be positive");
+	NLI_REQUIRE(C >= 1 && C <= 4, NLI_E_UNSUPPORTED, "images must have 1 to 4 channels");
+}
+
+extern "C" {
+
+const char *nli_version(void) { return "nli-gb300 1.0 (sm_103a)"; }
+
+const char *nli_status_string(int s)
+{
+	switch (s) {
+	case NLI_OK: return "ok";
+	case NLI_E_INVALID: return "invalid argument";
+	case NLI_E_EMPTY_SOURCE: return "empty source mask";
+	case NLI_E_CHANNELS: return "channels do not match";
+	case NLI_E_SHAPE: return "size mismatch";
+	case NLI_E_UNSUPPORTED: return "unsupported configuration";
+	case NLI_E_CUDA: return "CUDA error";
+	case NLI_E_TIMEOUT: return "device wait timed out";
+	case NLI_E_NOMEM: return "out of memory";
+	}
+	return "unknown status";
+}
+
+int nli_ctx_create(int device, nli_ctx **out)
+{
+	if (!out) return NLI_E_INVALID;
+	*out = nullptr;
+	nli_ctx *ctx = nullptr;
+	try {
+		ctx = new nli_ctx();
+		ctx->device = device;
+		NLI_CUDA(cudaSetDevice(device));
+		NLI_CUDA(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
+		ctx->stream = ctx->own_stream;
+		NLI_CUDA(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
+		NLI_CUDA(cudaMallocHost(&ctx->host_pinned, 4096));
+		NLI_CUDA(cudaMalloc(&ctx->status, sizeof(DevStatus)));
+		NLI_CUDA(cudaMemset(ctx->status, 0, sizeof(DevStatus)));
+	} catch (const Error &e) {
+		if (ctx) {
+			if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+			if (ctx->host_pinned) cudaFreeHost(ctx->host_pinned);
+			if (ctx->status) cudaFree(ctx->status);
+			delete ctx;
+		}
+		return e.status;
+	} catch (const std::bad_alloc &) {
+		delete ctx;
+		return NLI_E_NOMEM;
+	}
+	*out = ctx;
+	return NLI_OK;
+}
+
+int nli_ctx_destroy(nli_ctx *ctx)
+{
+	if (!ctx) return NLI_E_INVALID;
+	cudaSetDevice(ctx->device);
+	cudaStreamSynchronize(ctx->stream);
+	for (auto &kv : ctx->bufs) kv.second.release();
+	if (ctx->status) cudaFree(ctx->status);
+	if (ctx->host_pinned) cudaFreeHost(ctx->host_pinned);
+	if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+	delete ctx;
+	return NLI_OK;
+}
+
+int nli_ctx_set_stream(nli_ctx *ctx, void *stream)
+{
+	if (!ctx) return NLI_E_INVALID;
+	ctx->stream = (cudaStream_t)stream;
+	return NLI_OK;
+}
+
+int nli_set_seed(nli_ctx *ctx, uint64_t seed)
+{
+	if (!ctx) return NLI_E_INVALID;
+	ctx->seed = seed;
+	ctx->call_counter = 0;
+	return NLI_OK;
+}
+
+int nli_ctx_synchronize(nli_ctx *ctx)
+{
+	API_BEGIN(ctx)
+	NLI_CUDA(cudaStreamSynchronize(ctx->stream));
+	API_END(ctx)
+}
+
+const char *nli_last_error(nli_ctx *ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+int nli_gaussian_weights(int size_x, int size_y, float sigma_x, float sigma_y, float *host_out)
+{
+	if (size_x <= 0 || size_y <= 0 || !host_out) return NLI_E_INVALID;
+	std::vector<float> w = gaussian_weights_host(size_x, size_y, sigma_x, sigma_y);
+	std::memcpy(host_out, w.data(), sizeof(float) * w.size());
+	return NLI_OK;
+}
+
+float nli_subsampling_rate(float size_ratio, unsigned int scales)
+{
+	// float overloads of exp/log, as image_inpainting.cpp:203 resolves them
+	if (size_ratio < 0.0 || size_ratio > 1.0) return 0.0f;
+	return std::exp(std::log(size_ratio) / (float)(scales - 1));
+}
+
+int nli_sample_size(int size, float factor) { return sample_size_host(size, factor); }
+
+int nli_gradient(nli_ctx *ctx, const float *image, int W, int H, int C, float *gradient)
+{
+	API_BEGIN(ctx)
+	require_ptrs({image, gradient});
+	require_dims(W, H, C);
+	launch_gradient(ctx->stream, image, W, H, C, gradient);
+	API_END(ctx)
+}
+
+int nli_downsample_with_mask(nli_ctx *ctx, const float *image, const uint8_t *mask, int W, int H, int C,
+                             float factor, float threshold, int mask_val, float *out_image, uint8_t *out_mask)
+{
+	API_BEGIN(ctx)
+	require_ptrs({image, mask, out_image, out_mask});
+	require_dims(W, H, C);
+	NLI_REQUIRE(factor > 0 && factor < 1.0f, NLI_E_INVALID, "downsampling factor must be in (0, 1)");
+	downsample_with_mask_run(ctx, image, mask, W, H, C, factor, threshold, mask_val, out_image, out_mask);
+	API_END(ctx)
+}
+
+int nli_upsample(nli_ctx *ctx, const float *image, int W, int H, int C, int out_W, int out_H, float *out_image)
+{
+	API_BEGIN(ctx)
+	require_ptrs({image, out_image});
+	require_dims(W, H, C);
+	NLI_REQUIRE(out_W > 0 && out_H > 0, NLI_E_INVALID, "output sizes must be positive");
+	upsample_run(ctx, image, W, H, C, out_W, out_H, out_image);
+	API_END(ctx)
+}
+
+int nli_distance_transform(nli_ctx *ctx, const uint8_t *mask, int W, int H, float *distances)
+{
+	API_BEGIN(ctx)
+	require_ptrs({mask, distances});
+	require_dims(W, H, 1);
+	distance_transform_run(ctx, mask, W, H, distances);
+	API_END(ctx)
+}
+
+int nli_confidence_mask(nli_ctx *ctx, const uint8_t *mask, int W, int H, float decay_time, float asymptotic_value,
+                        float *confidence)
+{
+	API_BEGIN(ctx)
+	require_ptrs({mask, confidence});
+	require_dims(W, H, 1);
+	confidence_run(ctx, mask, W, H, decay_time, asymptotic_value, confidence);
+	API_END(ctx)
+}
+
+int nli_extended_domain(nli_ctx *ctx, const uint8_t *mask, int W, int H, int patch_x, int patch_y, uint8_t *extended)
+{
+	API_BEGIN(ctx)
+	require_ptrs({mask, extended});
+	require_dims(W, H, 1);
+	NLI_REQUIRE(patch_x >= 1 && patch_y >= 1, NLI_E_INVALID, "patch sizes must be positive");
+	extended_domain_run(ctx, mask, W, H, patch_x, patch_y, extended);
+	API_END(ctx)
+}
+
+int nli_scale_masks(nli_ctx *ctx, const uint8_t *extended, int W, int H, int margin, int erode, uint8_t *source,
+                    uint8_t *target, int *source_empty)
+{
+	API_BEGIN(ctx)
+	require_ptrs({extended, source, target});
+	require_dims(W, H, 1);
+	int *flag = ctx->buf<int>("scale_masks.flag", 1);
+	scale_masks_run(ctx, extended, W, H, margin, erode, source, target, flag);
+	if (source_empty) {
+		NLI_CUDA(cudaMemcpyAsync(ctx->host_pinned, flag, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+		NLI_CUDA(cudaStreamSynchronize(ctx->stream));
+		*source_empty = *(int *)ctx->host_pinned;
+	}
+	API_END(ctx)
+}
+
+int nli_poisson_init(nli_ctx *ctx, float *image, const uint8_t *mask, int W, int H, int C)
+{
+	API_BEGIN(ctx)
+	require_ptrs({image, mask});
+	require_dims(W, H, C);
+	poisson_init_run(ctx, image, mask, W, H, C);
+	API_END(ctx)
+}
+
+int nli_patchmatch(nli_ctx *ctx, const nli_distance_params *dist, const nli_patchmatch_params *pm,
+                   const float *source, const uint8_t *source_mask, int sW, int sH, const float *target,
+                   const uint8_t *target_mask, int tW, int tH, int C, const int32_t *init_nnf, int32_t *out_nnf,
+                   float *out_distance, double *energy)
+{
+	API_BEGIN(ctx)
+	require_ptrs({dist, pm, source, source_mask, target, target_mask, out_nnf});
+	require_dims(sW, sH, C);
+	require_dims(tW, tH, C);
+	NLI_REQUIRE(pm->iterations >= 0 && pm->random_shots >= 0, NLI_E_INVALID, "negative PatchMatch parameter");
+	patchmatch_run(ctx, *dist, *pm, source, source_mask, sW, sH, target, target_mask, tW, tH, C, init_nnf, out_nnf,
+	               out_distance, energy);
+	API_END(ctx)
+}
+
+int nli_update(nli_ctx *ctx, const nli_update_params *upd, float *image, const float *orig, const uint8_t *domain,
+               const uint8_t *ext_domain, const int32_t *nnf, const float *confidence, int W, int H, int C,
+               double *total_difference)
+{
+	API_BEGIN(ctx)
+	require_ptrs({upd, image, orig, domain, ext_domain, nnf});
+	require_dims(W, H, C);
+	double t = update_run(ctx, *upd, image, orig, domain, ext_domain, nnf, confidence, W, H, C);
+	if (total_difference) *total_difference = t;
+	API_END(ctx)
+}
+
+int nli_process_device(nli_ctx *ctx, const nli_process_params *params, const float *image, const uint8_t *mask, int W,
+                       int H, int C, float *out, nli_process_stats *stats)
+{
+	API_BEGIN(ctx)
+	require_ptrs({params, image, mask, out});
+	require_dims(W, H, C);
+	process_run(ctx, *params, image, mask, W, H, C, out, stats);
+	API_END(ctx)
+}
+
+int nli_process(nli_ctx *ctx, const nli_process_params *params, const float *image, const uint8_t *mask, int W, int H,
+                int C, float *out, nli_process_stats *stats)
+{
+	API_BEGIN(ctx)
+	require_ptrs({params, image, mask, out});
+	require_dims(W, H, C);
+	const size_t n = (size_t)W * H;
+	float *d_img = ctx->buf<float>("process.h_in", n * C);
+	uint8_t *d_mask = ctx->buf<uint8_t>("process.h_mask", n);
+	float *d_out = ctx->buf<float>("process.h_out", n * C);
+	NLI_CUDA(cudaMemcpyAsync(d_img, image, n * C * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+	NLI_CUDA(cudaMemcpyAsync(d_mask, mask, n, cudaMemcpyHostToDevice, ctx->stream));
+	process_run(ctx, *params, d_img, d_mask, W, H, C, d_out, stats);
+	NLI_CUDA(cudaMemcpyAsync(out, d_out, n * C * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+	NLI_CUDA(cudaStreamSynchronize(ctx->stream));
+	API_END(ctx)
+}
+
+}  // extern "C"

@@ -1,0 +1,138 @@
+// APatchDistance::calculate over explicit pair lists, and the exhaustive
+// nearest-neighbour search used to pin PatchMatch on small crops.  Both use
+// the reference-exact distance (nli_device.cuh, dist_exact).
+#include "nli_device.cuh"
+
+namespace nli {
+
+__global__ void k_distance_pairs(DistArgs a, const float *__restrict__ S, const float *__restrict__ GS, int sW,
+                                 const float *__restrict__ T, const float *__restrict__ GT, int tW,
+                                 const int4 *__restrict__ pairs, int n, float *__restrict__ out)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const int4 q = pairs[i];
+	out[i] = dist_exact(a, S, GS, sW, T, GT, tW, q.x, q.y, q.z, q.w);
+}
+
+// One block per target pixel; threads stride over the source pixels; the
+// block keeps the least distance, ties going to the lowest raster index.
+__global__ void k_bruteforce(DistArgs a, const float *__restrict__ S, const float *__restrict__ GS,
+                             const uint8_t *__restrict__ smask, int sW, int sH, const float *__restrict__ T,
+                             const float *__restrict__ GT, const uint8_t *__restrict__ tmask, int tW, int tH,
+                             int2 *__restrict__ nnf, float *__restrict__ dist)
+{
+	const int t = blockIdx.x;
+	const int tx = t % tW, ty = t / tW;
+	const bool valid_t = tmask[t] && tx - a.rx >= 0 && ty - a.ry >= 0 && tx + (a.px - a.rx) <= tW &&
+	                     ty + (a.py - a.ry) <= tH;
+	if (!valid_t) {
+		if (threadIdx.x == 0) {
+			nnf[t] = make_int2(-1, -1);
+			dist[t] = FLT_MAX;
+		}
+		return;
+	}
+	float best = FLT_MAX;
+	int best_i = INT_MAX;
+	const int ns = sW * sH;
+	for (int s = threadIdx.x; s < ns; s += blockDim.x) {
+		const int sx = s % sW, sy = s / sW;
+		if (!smask[s]) continue;
+		if (sx - a.rx < 0 || sy - a.ry < 0 || sx + (a.px - a.rx) > sW || sy + (a.py - a.ry) > sH) continue;
+		const float d = dist_exact(a, S, GS, sW, T, GT, tW, sx, sy, tx, ty);
+		if (d < best || (d == best && s < best_i)) {
+			best = d;
+			best_i = s;
+		}
+	}
+	__shared__ float sd[1024];
+	__shared__ int si[1024];
+	sd[threadIdx.x] = best;
+	si[threadIdx.x] = best_i;
+	__syncthreads();
+	for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+		if (threadIdx.x < o) {
+			const float d2 = sd[threadIdx.x + o];
+			const int i2 = si[threadIdx.x + o];
+			if (d2 < sd[threadIdx.x] || (d2 == sd[threadIdx.x] && i2 < si[threadIdx.x])) {
+				sd[threadIdx.x] = d2;
+				si[threadIdx.x] = i2;
+			}
+		}
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) {
+		const int b = si[0];
+		nnf[t] = (b == INT_MAX) ? make_int2(-1, -1) : make_int2(b % sW, b / sW);
+		dist[t] = sd[0];
+	}
+}
+
+static void gradients_for(nli_ctx *ctx, const nli_distance_params &p, const float *src, int sW, int sH,
+                          const float *tgt, int tW, int tH, int C, const float **gs, const float **gt)
+{
+	*gs = *gt = nullptr;
+	if (p.kind != NLI_DIST_L2_COMBINED && p.kind != NLI_DIST_L2_RGBD) return;
+	float *a = ctx->buf<float>("dist.gs", (size_t)sW * sH * 2 * C);
+	launch_gradient(ctx->stream, src, sW, sH, C, a);
+	*gs = a;
+	if (tgt == src && tW == sW && tH == sH) {
+		*gt = a;
+		return;
+	}
+	float *b = ctx->buf<float>("dist.gt", (size_t)tW * tH * 2 * C);
+	launch_gradient(ctx->stream, tgt, tW, tH, C, b);
+	*gt = b;
+}
+
+}  // namespace nli
+
+using namespace nli;
+
+extern "C" int nli_distance_pairs(nli_ctx *ctx, const nli_distance_params *dist, const float *source, int sW, int sH,
+                                  const float *target, int tW, int tH, int C, const int32_t *pairs, int n, float *out)
+{
+	if (!ctx) return NLI_E_INVALID;
+	try {
+		NLI_CUDA(cudaSetDevice(ctx->device));
+		NLI_REQUIRE(dist && source && target && out && (pairs || n == 0), NLI_E_INVALID, "null pointer argument");
+		NLI_REQUIRE(sW > 0 && sH > 0 && tW > 0 && tH > 0 && n >= 0, NLI_E_INVALID, "bad sizes");
+		DistArgs a;
+		fill_dist_args(a, *dist, C);
+		if (n == 0) return NLI_OK;
+		const float *gs, *gt;
+		gradients_for(ctx, *dist, source, sW, sH, target, tW, tH, C, &gs, &gt);
+		k_distance_pairs<<<(n + 127) / 128, 128, 0, ctx->stream>>>(a, source, gs, sW, target, gt, tW,
+		                                                            reinterpret_cast<const int4 *>(pairs), n, out);
+		NLI_CHECK_LAUNCH();
+	} catch (const Error &e) {
+		ctx->last_error = e.message;
+		return e.status;
+	}
+	return NLI_OK;
+}
+
+extern "C" int nli_bruteforce_nnf(nli_ctx *ctx, const nli_distance_params *dist, const float *source,
+                                  const uint8_t *source_mask, int sW, int sH, const float *target,
+                                  const uint8_t *target_mask, int tW, int tH, int C, int32_t *nnf, float *distance)
+{
+	if (!ctx) return NLI_E_INVALID;
+	try {
+		NLI_CUDA(cudaSetDevice(ctx->device));
+		NLI_REQUIRE(dist && source && source_mask && target && target_mask && nnf && distance, NLI_E_INVALID,
+		            "null pointer argument");
+		NLI_REQUIRE(sW > 0 && sH > 0 && tW > 0 && tH > 0, NLI_E_INVALID, "bad sizes");
+		DistArgs a;
+		fill_dist_args(a, *dist, C);
+		const float *gs, *gt;
+		gradients_for(ctx, *dist, source, sW, sH, target, tW, tH, C, &gs, &gt);
+		k_bruteforce<<<tW * tH, 256, 0, ctx->stream>>>(a, source, gs, source_mask, sW, sH, target, gt, target_mask,
+		                                                tW, tH, reinterpret_cast<int2 *>(nnf), distance);
+		NLI_CHECK_LAUNCH();
+	} catch (const Error &e) {
+		ctx->last_error = e.message;
+		return e.status;
+	}
+	return NLI_OK;
+}

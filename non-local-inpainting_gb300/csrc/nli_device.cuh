@@ -1,0 +1,296 @@
+// Device-side helpers: reference-exact arithmetic, the counter-based RNG,
+// the patch distances, reductions and a bounded grid barrier.
+#pragma once
+
+#include <cfloat>
+#include <cstdint>
+
+#include "nli_internal.cuh"
+
+namespace nli {
+
+// ------------------------------------------------------------------------
+// Reference-exact arithmetic.  The reference is compiled for the host with
+// separate IEEE roundings for every product and sum (no fused multiply-add);
+// these wrappers keep the CUDA compiler from contracting them.
+__device__ __forceinline__ float fm(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
+
+// ------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as
+// easy as 1, 2, 3", SC 2011): 10 rounds of two 32x32->64 multiplies with the
+// published multipliers and Weyl key increments.
+__device__ __forceinline__ uint4 philox(uint4 c, uint2 k)
+{
+#pragma unroll
+	for (int i = 0; i < 10; i++) {
+		uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+		uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+		c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+		k.x += 0x9E3779B9u;
+		k.y += 0xBB67AE85u;
+	}
+	return c;
+}
+
+// A stream of 32-bit draws for one (pixel, sweep) pair: four draws per
+// Philox block, counter = (pixel, sweep, block index, 0).
+struct Rng {
+	uint2 key;
+	uint32_t pixel, sweep, block;
+	uint4 cur;
+	int used;
+	__device__ Rng(uint2 k, uint32_t p, uint32_t s) : key(k), pixel(p), sweep(s), block(0), used(4) {}
+	__device__ __forceinline__ uint32_t next()
+	{
+		if (used == 4) {
+			cur = philox(make_uint4(pixel, sweep, block++, 0x6e6c6900u), key);
+			used = 0;
+		}
+		uint32_t r = (used == 0) ? cur.x : (used == 1) ? cur.y : (used == 2) ? cur.z : cur.w;
+		used++;
+		return r;
+	}
+	// draw in [0, n), n >= 1 (the reference uses rand() % n)
+	__device__ __forceinline__ int below(int n) { return (int)(next() % (uint32_t)n); }
+};
+
+// ------------------------------------------------------------------------
+// Patch distances, reference-exact variant.  Reads the image and its
+// gradient in the reference layouts (HWC and 2C-interleaved) and follows
+// l2_combined_patch_distance.cpp:39-148, l2_rgbd_patch_distance.cpp:41-117,
+// l2_norm_patch_distance.cpp:22-104 and l1_norm_patch_distance.cpp:22-105:
+// float per-tap norms, float weight*norm products, double sums for the
+// L2Combined/L2RGBD kinds, float sums for L2Norm/L1Norm.
+__device__ inline float dist_exact(const DistArgs &a, const float *__restrict__ S,
+                                   const float *__restrict__ GS, int sW, const float *__restrict__ T,
+                                   const float *__restrict__ GT, int tW, int sx, int sy, int tx, int ty)
+{
+	const int C = a.C;
+	const float *pw = a.weights;
+	if (a.kind == NLI_DIST_L2_COMBINED || a.kind == NLI_DIST_L2_RGBD) {
+		double D = 0.0, G = 0.0, Dd = 0.0, Gd = 0.0;
+		for (int dy = -a.ry; dy < a.py - a.ry; dy++)
+			for (int dx = -a.rx; dx < a.px - a.rx; dx++, ++pw) {
+				const float w = *pw;
+				const int si = C * (sW * (sy + dy) + (sx + dx));
+				const int ti = C * (tW * (ty + dy) + (tx + dx));
+				if (a.kind == NLI_DIST_L2_COMBINED && (C == 3 || C == 1)) {
+					float norm, gnorm;
+					if (C == 3) {
+						float d0 = fs(S[si], T[ti]), d1 = fs(S[si + 1], T[ti + 1]), d2 = fs(S[si + 2], T[ti + 2]);
+						norm = fa(fa(fm(d0, d0), fm(d1, d1)), fm(d2, d2));
+						float e0 = fs(GS[2 * si], GT[2 * ti]), e1 = fs(GS[2 * si + 1], GT[2 * ti + 1]);
+						float e2 = fs(GS[2 * si + 2], GT[2 * ti + 2]), e3 = fs(GS[2 * si + 3], GT[2 * ti + 3]);
+						float e4 = fs(GS[2 * si + 4], GT[2 * ti + 4]), e5 = fs(GS[2 * si + 5], GT[2 * ti + 5]);
+						gnorm = fa(fa(fa(fa(fa(fm(e0, e0), fm(e1, e1)), fm(e2, e2)), fm(e3, e3)), fm(e4, e4)),
+						           fm(e5, e5));
+					} else {
+						float d0 = fs(S[si], T[ti]);
+						norm = fm(d0, d0);
+						float e0 = fs(GS[2 * si], GT[2 * ti]), e1 = fs(GS[2 * si + 1], GT[2 * ti + 1]);
+						gnorm = fa(fm(e0, e0), fm(e1, e1));
+					}
+					D = da(D, (double)fm(w, norm));
+					G = da(G, (double)fm(w, gnorm));
+				} else {
+					double n = 0.0, g = 0.0, nd = 0.0, gd = 0.0;
+					for (int c = 0; c < C; c++) {
+						float d = fs(S[si + c], T[ti + c]);
+						float ex = fs(GS[2 * (si + c)], GT[2 * (ti + c)]);
+						float ey = fs(GS[2 * (si + c) + 1], GT[2 * (ti + c) + 1]);
+						float gg = fa(fm(ex, ex), fm(ey, ey));
+						if (a.kind == NLI_DIST_L2_RGBD && c == 3) {
+							nd = da(nd, (double)fm(d, d));
+							gd = da(gd, (double)gg);
+						} else {
+							n = da(n, (double)fm(d, d));
+							g = da(g, (double)gg);
+						}
+					}
+					D = da(D, dm((double)w, n));
+					G = da(G, dm((double)w, g));
+					Dd = da(Dd, dm((double)w, nd));
+					Gd = da(Gd, dm((double)w, gd));
+				}
+			}
+		const double P = (double)((unsigned)a.px * (unsigned)a.py);
+		double r = da(dm((double)a.lambda, D), dm((double)fs(1.0f, a.lambda), G));
+		if (a.kind == NLI_DIST_L2_RGBD)
+			r = da(da(r, dm((double)a.lambda_d, Dd)), dm((double)fs(1.0f, a.lambda_d), Gd));
+		return __double2float_rn(__ddiv_rn(r, P));
+	}
+	// L2Norm / L1Norm: float accumulator
+	float D = 0.0f;
+	for (int dy = -a.ry; dy < a.py - a.ry; dy++)
+		for (int dx = -a.rx; dx < a.px - a.rx; dx++, ++pw) {
+			const float w = *pw;
+			const int si = C * (sW * (sy + dy) + (sx + dx));
+			const int ti = C * (tW * (ty + dy) + (tx + dx));
+			float norm;
+			if (a.kind == NLI_DIST_L2_NORM) {
+				if (C == 3) {
+					float d0 = fs(S[si], T[ti]), d1 = fs(S[si + 1], T[ti + 1]), d2 = fs(S[si + 2], T[ti + 2]);
+					norm = fa(fa(fm(d0, d0), fm(d1, d1)), fm(d2, d2));
+				} else if (C == 1) {
+					float d0 = fs(S[si], T[ti]);
+					norm = fm(d0, d0);
+				} else {
+					norm = 0.0f;
+					for (int c = 0; c < C; c++) {
+						float d = fs(S[si + c], T[ti + c]);
+						norm = fa(norm, fm(d, d));
+					}
+				}
+			} else {
+				if (C == 3) {
+					norm = fa(fa(fabsf(fs(S[si], T[ti])), fabsf(fs(S[si + 1], T[ti + 1]))),
+					          fabsf(fs(S[si + 2], T[ti + 2])));
+				} else {
+					norm = 0.0f;
+					for (int c = 0; c < C; c++) norm = fa(norm, fabsf(fs(S[si + c], T[ti + c])));
+				}
+			}
+			D = fa(D, fm(w, norm));
+		}
+	return __fdiv_rn(D, (float)((unsigned)a.px * (unsigned)a.py));
+}
+
+// ------------------------------------------------------------------------
+// Patch distances, fast single-precision variant used inside PatchMatch.
+// Reads the packed feature image (NF4 float4 per pixel, see
+// launch_features) and accumulates in float with fused multiply-adds.  Its
+// relative deviation from the reference-exact value is ~1e-6.
+template <int KIND, int C, int NF4>
+__device__ __forceinline__ float dist_fast(const DistArgs &a, const float4 *__restrict__ fsrc, int sW,
+                                           const float4 *__restrict__ ftgt, int tW, int sx, int sy, int tx,
+                                           int ty)
+{
+	float D = 0.f, G = 0.f, Dd = 0.f, Gd = 0.f;
+	const float *pw = a.weights;
+	for (int dy = -a.ry; dy < a.py - a.ry; dy++) {
+		const float4 *sp = fsrc + ((size_t)(sy + dy) * sW + (sx - a.rx)) * NF4;
+		const float4 *tp = ftgt + ((size_t)(ty + dy) * tW + (tx - a.rx)) * NF4;
+#pragma unroll 3
+		for (int dx = 0; dx < a.px; dx++, ++pw) {
+			float f[4 * NF4];
+#pragma unroll
+			for (int k = 0; k < NF4; k++) {
+				float4 s4 = __ldg(sp + dx * NF4 + k);
+				float4 t4 = __ldg(tp + dx * NF4 + k);
+				f[4 * k + 0] = s4.x - t4.x;
+				f[4 * k + 1] = s4.y - t4.y;
+				f[4 * k + 2] = s4.z - t4.z;
+				f[4 * k + 3] = s4.w - t4.w;
+			}
+			const float w = *pw;
+			if (KIND == NLI_DIST_L1_NORM) {
+				float n = 0.f;
+#pragma unroll
+				for (int c = 0; c < C; c++) n += fabsf(f[c]);
+				D = fmaf(w, n, D);
+			} else if (KIND == NLI_DIST_L2_NORM) {
+				float n = 0.f;
+#pragma unroll
+				for (int c = 0; c < C; c++) n = fmaf(f[c], f[c], n);
+				D = fmaf(w, n, D);
+			} else if (KIND == NLI_DIST_L2_RGBD) {
+				float n = 0.f, g = 0.f;
+#pragma unroll
+				for (int c = 0; c < 3; c++) n = fmaf(f[c], f[c], n);
+#pragma unroll
+				for (int c = 0; c < 6; c++) g = fmaf(f[4 + c], f[4 + c], g);
+				D = fmaf(w, n, D);
+				G = fmaf(w, g, G);
+				Dd = fmaf(w, f[3] * f[3], Dd);
+				Gd = fmaf(w, fmaf(f[10], f[10], f[11] * f[11]), Gd);
+			} else {
+				float n = 0.f, g = 0.f;
+#pragma unroll
+				for (int c = 0; c < C; c++) n = fmaf(f[c], f[c], n);
+#pragma unroll
+				for (int c = 0; c < 2 * C; c++) g = fmaf(f[C + c], f[C + c], g);
+				D = fmaf(w, n, D);
+				G = fmaf(w, g, G);
+			}
+		}
+	}
+	const float invP = 1.0f / (float)(a.px * a.py);
+	if (KIND == NLI_DIST_L1_NORM || KIND == NLI_DIST_L2_NORM) return D * invP;
+	float r = a.lambda * D + (1.0f - a.lambda) * G;
+	if (KIND == NLI_DIST_L2_RGBD) r += a.lambda_d * Dd + (1.0f - a.lambda_d) * Gd;
+	return r * invP;
+}
+
+// ------------------------------------------------------------------------
+// Reductions.
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+	return v;
+}
+
+__device__ __forceinline__ float warp_sum(float v)
+{
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+	return v;
+}
+
+// Sum over the block (result valid in thread 0); fixed order, so repeatable.
+template <int BLOCK>
+__device__ __forceinline__ double block_sum(double v, double *smem /* BLOCK/32 */)
+{
+	v = warp_sum(v);
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	if (lane == 0) smem[wid] = v;
+	__syncthreads();
+	double t = 0.0;
+	if (wid == 0) {
+		t = (lane < BLOCK / 32) ? smem[lane] : 0.0;
+		t = warp_sum(t);
+	}
+	__syncthreads();
+	return t;
+}
+
+// ------------------------------------------------------------------------
+// Grid-wide barrier for cooperatively launched kernels (all blocks are
+// co-resident).  Spins at most `limit` polls; on expiry it records a
+// timeout in the status block and returns false so the kernel can leave.
+__device__ __forceinline__ bool grid_barrier(DevStatus *st, unsigned nblocks, unsigned limit = 1u << 26)
+{
+	__syncthreads();
+	bool ok = true;
+	if (threadIdx.x == 0) {
+		volatile unsigned *gen = &st->barrier_gen;
+		unsigned g = *gen;
+		__threadfence();
+		if (atomicAdd(&st->barrier_count, 1u) == nblocks - 1) {
+			st->barrier_count = 0;
+			__threadfence();
+			atomicExch(&st->barrier_gen, g + 1);
+		} else {
+			unsigned polls = 0;
+			while (*gen == g) {
+				if (++polls > limit || *(volatile int *)&st->timeout) {
+					atomicExch(&st->timeout, 1);
+					ok = false;
+					break;
+				}
+				__nanosleep(32);
+			}
+		}
+		__threadfence();
+	}
+	__syncthreads();
+	// every block learns about a timeout at its next barrier at the latest
+	return ok && !*(volatile int *)&st->timeout;
+}
+
+}  // namespace nli

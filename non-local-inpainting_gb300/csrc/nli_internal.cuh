@@ -1,0 +1,170 @@
+// Internal declarations shared by the CUDA translation units of the
+// GB300 (sm_103a) non-local inpainting library.  Not part of the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "nli.h"
+
+namespace nli {
+
+// ---------------------------------------------------------------- errors
+struct Error {
+	int status;
+	std::string message;
+};
+
+#define NLI_CUDA(call)                                                                     \
+	do {                                                                                   \
+		cudaError_t e_ = (call);                                                           \
+		if (e_ != cudaSuccess)                                                             \
+			throw ::nli::Error{e_ == cudaErrorMemoryAllocation ? NLI_E_NOMEM : NLI_E_CUDA, \
+			                   std::string(#call) + ": " + cudaGetErrorString(e_)};        \
+	} while (0)
+
+#define NLI_CHECK_LAUNCH() NLI_CUDA(cudaGetLastError())
+
+#define NLI_REQUIRE(cond, status, msg)                  \
+	do {                                                \
+		if (!(cond)) throw ::nli::Error{(status), (msg)}; \
+	} while (0)
+
+// ------------------------------------------------------------- workspace
+// Grow-only device buffer.  Reallocation happens only when a larger size is
+// requested, so steady-state calls allocate nothing.
+struct DevBuf {
+	void *ptr = nullptr;
+	size_t bytes = 0;
+	void *ensure(size_t n)
+	{
+		if (n > bytes) {
+			if (ptr) NLI_CUDA(cudaFree(ptr));
+			ptr = nullptr;
+			bytes = 0;
+			size_t want = n + n / 8 + 256;
+			NLI_CUDA(cudaMalloc(&ptr, want));
+			bytes = want;
+		}
+		return ptr;
+	}
+	void release()
+	{
+		if (ptr) cudaFree(ptr);
+		ptr = nullptr;
+		bytes = 0;
+	}
+};
+
+// Device-side status words written by kernels that wait (grid barriers).
+struct DevStatus {
+	unsigned int barrier_count;
+	unsigned int barrier_gen;
+	int timeout;
+	int pad;
+};
+
+}  // namespace nli
+
+struct nli_ctx {
+	int device = 0;
+	cudaStream_t own_stream = nullptr;
+	cudaStream_t stream = nullptr;
+	uint64_t seed = 0x9e3779b97f4a7c15ULL;
+	uint64_t call_counter = 0;
+	std::string last_error;
+	int num_sms = 0;
+	std::map<std::string, nli::DevBuf> bufs;
+	// pinned host staging for small results
+	void *host_pinned = nullptr;
+	// device status block
+	nli::DevStatus *status = nullptr;
+	// running counters (for stats)
+	int64_t candidates = 0;
+	int64_t cg_iterations = 0;
+
+	template <class T>
+	T *buf(const std::string &name, size_t count)
+	{
+		return static_cast<T *>(bufs[name].ensure(count * sizeof(T)));
+	}
+};
+
+namespace nli {
+
+// ------------------------------------------------------------ parameters
+constexpr int kMaxTaps = NLI_MAX_PATCH * NLI_MAX_PATCH;
+
+// Everything a distance evaluation needs, passed by value to kernels.
+struct DistArgs {
+	int kind;
+	int px, py, rx, ry;  // patch size and radius (radius = size / 2)
+	int C;               // image channels
+	int nf4;             // float4 per pixel in the feature image
+	float lambda, lambda_d;
+	float weights[kMaxTaps];  // Gaussian patch weights, row-major
+};
+
+// ---------------------------------------------------------- host helpers
+std::vector<float> gaussian_weights_host(unsigned sx, unsigned sy, float sigma_x, float sigma_y);
+void fill_dist_args(DistArgs &a, const nli_distance_params &p, int C);
+int feature_float4s(int kind, int C);
+
+// ------------------------------------------------------------- launchers
+// gradient.cu
+void launch_gradient(cudaStream_t s, const float *img, int W, int H, int C, float *grad);
+// Feature image for the distances: per pixel nf4 float4 =
+// [u_0..u_{C-1}, gx_0, gy_0, ..., gx_{C-1}, gy_{C-1}, 0-padding] (colour only
+// for the L2Norm/L1Norm kinds).
+void launch_features(cudaStream_t s, int kind, const float *img, int W, int H, int C, float4 *feat);
+
+// compact.cu: raster-order list of the pixels with mask != 0; returns count
+int compact_mask(nli_ctx *ctx, const uint8_t *mask, int W, int H, int32_t *list, const char *tag);
+
+// reductions
+void launch_sum_partials(cudaStream_t s, const double *partials, int n, double *out);
+
+// patchmatch.cu
+struct PmStats {
+	double energy;
+};
+void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patchmatch_params &pm,
+                    const float *src, const uint8_t *smask, int sW, int sH, const float *tgt,
+                    const uint8_t *tmask, int tW, int tH, int C, const int32_t *init_nnf,
+                    int32_t *out_nnf, float *out_dist, double *energy, const int32_t *tlist = nullptr,
+                    int n_target = -1);
+
+// update.cu
+double update_run(nli_ctx *ctx, const nli_update_params &up, float *image, const float *orig,
+                  const uint8_t *dom, const uint8_t *ext, const int32_t *nnf, const float *conf, int W,
+                  int H, int C, const int32_t *hole_list = nullptr, int n_hole = -1,
+                  bool read_back = true);
+
+// pyramid.cu
+void downsample_with_mask_run(nli_ctx *ctx, const float *img, const uint8_t *mask, int W, int H, int C,
+                              float factor, float threshold, int mask_val, float *out_img,
+                              uint8_t *out_mask);
+void downsample_image_run(nli_ctx *ctx, const float *img, int W, int H, int C, float factor, float *out);
+void downsample_mask_run(nli_ctx *ctx, const uint8_t *mask, int W, int H, float factor, float threshold,
+                         uint8_t *out);
+void upsample_run(nli_ctx *ctx, const float *img, int W, int H, int C, int oW, int oH, float *out);
+void distance_transform_run(nli_ctx *ctx, const uint8_t *mask, int W, int H, float *out);
+void confidence_run(nli_ctx *ctx, const uint8_t *mask, int W, int H, float decay, float asym, float *out);
+void extended_domain_run(nli_ctx *ctx, const uint8_t *mask, int W, int H, int px, int py, uint8_t *out);
+void scale_masks_run(nli_ctx *ctx, const uint8_t *ext, int W, int H, int margin, int erode, uint8_t *src,
+                     uint8_t *tgt, int *empty_dev);
+void poisson_init_run(nli_ctx *ctx, float *img, const uint8_t *mask, int W, int H, int C);
+int sample_size_host(unsigned size, float factor);
+
+// process.cu
+void process_run(nli_ctx *ctx, const nli_process_params &p, const float *img, const uint8_t *mask, int W,
+                 int H, int C, float *out, nli_process_stats *stats);
+
+}  // namespace nli
