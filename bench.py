@@ -1,0 +1,363 @@
+#!/usr/bin/env python
+"""Benchmark: inpainted Mpix/s of the multiscale non-local inpainting path.
+
+A step is one ImageInpainting::process of the 512x512 nlpoisson workload
+(Voronoi texture, 6-ellipse hole of ~15%, L2Combined, lambda 0.05, patch 9,
+scales 8, coarse 0.1, CG tolerance 1e-4, seeded synthetic input).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value`: Mpix/s with the input already in HBM (nli_process_device), timed
+with CUDA events on the launching stream; L2 (129 MB) is flushed with a
+256 MB write between timed steps.  `e2e`: the same through nli_process with
+pinned host buffers (host->device input copy and device->host result copy
+inside the timed region).  N > 1 runs independent replicas, one per GPU
+(the path has no exchange step), weak scaling.
+
+The reference arm (--impl reference) times the reference algorithm on the
+host cores: the CPU restatement of the reference (oracle/, bit-identical to
+the reference's serial build; its PatchMatch is the reference's OpenMP
+variant) on a bounded sample per step -- one PatchMatch and one update on
+every pyramid scale -- scaled to a whole process() by the reference's own
+per-scale iteration counts of this workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import __graft_entry__ as ge  # noqa: E402
+
+METRIC = "inpainted Mpix/s on 1 GB300, batched vs plain GPU path, ≤0.1 dB PSNR gap to ref"
+UNIT = "Mpix/s"
+# algorithmic FP32 work of one patch distance, P = 9: 31 P^2 + 8 (C = 3,
+# L2Combined: 9 differences, 9 squares/FMAs and 2 weighted FMAs per tap)
+FLOP_PER_CANDIDATE = 31 * 81 + 8
+# algorithmic bytes of one CG iteration per unknown and channel: read d, a1,
+# a2-links, x, r, q; write x, r, d (float32), as counted for the roofline
+CG_BYTES_PER_UNKNOWN_ITER = 32
+L2_FLUSH_BYTES = 256 << 20
+COUNTS = os.path.join(ROOT, "tests", "golden", "config2_reference_counts.json")
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+TRAFFIC = os.path.join(ROOT, "profiles", "pm_sweep_traffic.json")
+
+
+def workload_desc():
+    return ("512x512 RGB float32 Voronoi (40 seeds) + oriented sinusoids, union of 6 ellipses (~15% hole); "
+            "nlpoisson + L2Combined, lambda 0.05, psigma 10000, patch 9, scales 8, coarse 0.1, CG tol 1e-4, "
+            "iters 200, tol 0.1, conft 5, confa 0.1, init poisson, PatchMatch 10 sweeps / 30 shots")
+
+
+def workload(seed=0):
+    pkg = ge.package()
+    from nli_gb300 import workloads as wl
+    return wl.config2(seed=seed)
+
+
+class Clocks:
+    """nvidia-smi samples (every 200 ms) while the timed region runs."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out = self.proc.communicate(timeout=5)[0]
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out = self.proc.communicate()[0]
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def reference_counts():
+    """Per-scale PatchMatch / update call counts of the reference on this
+    workload (serial run, committed fixture), finest scale first."""
+    if os.path.exists(COUNTS):
+        with open(COUNTS) as f:
+            c = json.load(f)
+        return c["iterations"], "reference run (seed %d)" % c.get("seed", 0)
+    return None, None
+
+
+def cpu_sample(img, mask, p, iterations):
+    """Times one PatchMatch (OpenMP, all host threads) and one update on
+    every scale with the oracle restatement and returns (estimated seconds
+    of a whole process(), wall seconds spent, threads)."""
+    from oracle import oracle as O
+    orc = O.Oracle()
+    S = p.scales
+    imgs, masks = [np.asarray(img, np.float32)], [np.asarray(mask, np.uint8)]
+    for i in range(1, S):
+        a, b = orc.downsample_with_mask(imgs[-1], masks[-1], p.subsampling_rate, 0.4, False)
+        imgs.append(a)
+        masks.append(b)
+    t_pm, t_up = [], []
+    wall0 = time.perf_counter()
+    for lvl in range(S):
+        im = orc.poisson_init(imgs[lvl], masks[lvl])
+        ext = orc.extended_domain(masks[lvl], p.update.patch_x, p.update.patch_y)
+        src, tgt, _ = orc.scale_masks(ext, p.update.patch_x // 2, True)
+        conf = orc.confidence_mask(masks[lvl], p.conf_decay_time, p.conf_asymptotic)
+        t0 = time.perf_counter()
+        nnf = orc.patchmatch(p.distance, p.patchmatch, im, src, im, tgt, seed=lvl, parallel=True)[0]
+        t1 = time.perf_counter()
+        orc.update(p.update, im, im, masks[lvl], ext, nnf, conf)
+        t2 = time.perf_counter()
+        t_pm.append(t1 - t0)
+        t_up.append(t2 - t1)
+    wall = time.perf_counter() - wall0
+    est = 0.0
+    for lvl in range(S):
+        est += iterations[lvl] * (t_pm[lvl] + t_up[lvl])
+        if lvl < S - 1:  # propagate_weights into this scale: 2 PatchMatch + 1 update
+            est += t_pm[lvl + 1] + t_pm[lvl] + t_up[lvl]
+    return est, wall, orc.max_threads
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return 0
+    img, mask, p = workload()
+    iters, source = reference_counts()
+    if iters is None:
+        print(json.dumps({"impl": "reference", "unavailable": "per-scale iteration counts of the reference run "
+                          "(tests/golden/config2_reference_counts.json) are missing"}))
+        return 0
+    mpix = img.shape[0] * img.shape[1] / 1e6
+    for _ in range(args.warmup):
+        cpu_sample(img, mask, p, iters)
+    ests, walls, threads = [], [], 1
+    for _ in range(args.steps):
+        est, wall, threads = cpu_sample(img, mask, p, iters)
+        ests.append(est)
+        walls.append(wall)
+    est = statistics.median(ests)
+    value = mpix / est
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(walls), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 (reference arithmetic)", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": workload_desc(), "path": "reference algorithm on host cores"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "per step: 1 PatchMatch (OpenMP) + 1 NL-Poisson update on each of the 8 scales, "
+                                   "scaled by the per-scale call counts of the %s; estimated %.1f s per "
+                                   "process()" % (source, est)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_setup()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    pkg = ge.package()
+    ge.build() if not os.path.exists(pkg.LIB_PATH) else None
+    ctx = pkg.Context(local)
+    ctx.set_seed(1234 + rank)
+    img, mask, p = workload()
+    H, W, C = img.shape
+    mpix = W * H / 1e6
+    dev = "cuda:%d" % local
+    d_img = torch.from_numpy(img).to(dev)
+    d_mask = torch.from_numpy(mask).to(dev)
+    d_out = torch.empty_like(d_img)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    def timed(fn, k, profile=False):
+        ms = []
+        for i in range(k):
+            flush.fill_(i & 0xFF)  # evict L2 between steps (outside the timed events)
+            torch.cuda.synchronize()
+            barrier()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        return ms
+
+    def step():
+        ctx.process_device(d_img, d_mask, p, out=d_out)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    c0 = ctx.counters()
+    l0 = ctx.launch_count()
+    ctx.set_profiling(True)
+    clocks = Clocks(local)
+    clocks.start()
+    ms = timed(step, args.steps)
+    clk = clocks.stop()
+    prof = ctx.profile()
+    ctx.set_profiling(False)
+    launches = ctx.launch_count() - l0
+    c1 = ctx.counters()
+    total_ms = sum(ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps * mpix / (total_ms / 1e3)
+
+    # end to end: pinned host buffers, copies inside the timed region
+    import ctypes as ct
+    h_img = torch.from_numpy(img).pin_memory()
+    h_mask = torch.from_numpy(mask).pin_memory()
+    h_out = torch.empty_like(h_img).pin_memory()
+    st = pkg.ProcessStats()
+
+    def e2e_step():
+        rc = ctx.lib.nli_process(ctx.h, ct.byref(p), ct.c_void_p(h_img.data_ptr()), ct.c_void_p(h_mask.data_ptr()),
+                                 W, H, C, ct.c_void_p(h_out.data_ptr()), ct.byref(st))
+        if rc != 0:
+            raise RuntimeError(ctx.lib.nli_last_error(ctx.h).decode())
+
+    e2e_step()
+    ems = timed(e2e_step, args.steps)
+    e_total = sum(ems)
+    if world > 1:
+        t = torch.tensor([e_total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e_total = float(t.item())
+    e2e_value = world * args.steps * mpix / (e_total / 1e3)
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return 0
+
+    # roofline of the dominant kernel, from the events timed inside the steps
+    peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
+    sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    n_sm = torch.cuda.get_device_properties(local).multi_processor_count
+    fp32_peak = n_sm * 128 * 2 * sm_mhz * 1e6 / 1e12  # TFLOP/s: FP32 lanes x FMA at the sampled clock
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    dom = max(prof.items(), key=lambda kv: kv[1][1]) if prof else ("none", (0, 0.0))
+    cand = c1["candidates"] - c0["candidates"]
+    pm_ms = sum(v[1] for k, v in prof.items() if k.startswith("pm_"))
+    pm_launches = sum(v[0] for k, v in prof.items() if k.startswith("pm_"))
+    traffic = None
+    if os.path.exists(TRAFFIC):
+        traffic = json.load(open(TRAFFIC)).get("bytes_per_launch")
+    pm_tflops = cand * FLOP_PER_CANDIDATE / (pm_ms / 1e3) / 1e12 if pm_ms > 0 else 0.0
+    roofline = {"kernel": "k_pm_init + k_pm_sweep (PatchMatch)", "bound": "fp32", "achieved": pm_tflops,
+                "peak": fp32_peak, "unit": "TFLOP/s", "frac": pm_tflops / fp32_peak if fp32_peak else None,
+                "traffic": traffic, "launches": pm_launches, "ms": pm_ms,
+                "peak_source": "nominal FP32 (%d SMs x 128 lanes x 2 FLOP) at the sampled median SM clock %.0f MHz; "
+                               "MEASURED_PEAKS.json has no FP32 figure" % (n_sm, sm_mhz),
+                "flop_per_candidate": FLOP_PER_CANDIDATE, "candidates": cand}
+    cg = prof.get("poisson_cg", (0, 0.0))
+    cg_work = c1["cg_unknown_iterations"] - c0["cg_unknown_iterations"]
+    cg_gbs = cg_work * CG_BYTES_PER_UNKNOWN_ITER / (cg[1] / 1e3) / 1e9 if cg[1] > 0 else 0.0
+    kernels = {k: {"launches": v[0], "ms": v[1], "share": v[1] / total_ms if total_ms else None}
+               for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
+    cpu = None
+    if world == 1 and not args.no_cpu_baseline:
+        iters, source = reference_counts()
+        if iters is None:
+            iters, source = list(st.iterations[:p.scales]), "GPU run (reference counts missing)"
+        est, wall, threads = cpu_sample(img, mask, p, iters)
+        cpu = {"value": mpix / est, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "1 PatchMatch (OpenMP) + 1 NL-Poisson update on each of the 8 scales (%.1f s wall), scaled "
+                         "by the per-scale call counts of the %s: %.1f s per process()" % (wall, source, est)}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 CG inner products)", "data": "synthetic",
+        "config": {"workload": workload_desc(), "path": "plain (one process() per step)",
+                   "l2": "flushed between timed steps (256 MB write)", "parallelism": "replicas x%d" % world},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(img.nbytes + mask.nbytes),
+                "d2h_bytes_per_step": int(img.nbytes), "ms_per_step": e_total / args.steps},
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "roofline": roofline,
+        "roofline_cg": {"kernel": "k_poisson_cg", "bound": "hbm", "achieved": cg_gbs, "peak": hbm_peak,
+                        "unit": "GB/s", "frac": cg_gbs / hbm_peak if hbm_peak else None,
+                        "bytes_per_unknown_iteration": CG_BYTES_PER_UNKNOWN_ITER, "peak_source": "measured"},
+        "kernels": kernels,
+        "dominant_kernel": dom[0],
+        "cpu_baseline": cpu,
+        "process_stats": {"iterations": list(st.iterations[:p.scales]), "patchmatch_calls": st.patchmatch_calls,
+                          "update_calls": st.update_calls, "cg_iterations": st.cg_iterations},
+    }
+    print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -150,6 +150,21 @@ int nli_ctx_synchronize(nli_ctx *ctx);
 /* Message of the last failing call on this context (never NULL). */
 const char *nli_last_error(nli_ctx *ctx);
 
+/* ---- observability (the reference's METRICS / progress prints,
+ * patch_match.cpp:383-507, image_inpainting.cpp:396-407) ------------------- */
+/* Number of kernels this library has launched in this process. */
+int64_t nli_launch_count(void);
+/* Turns per-kernel GPU timing on or off (CUDA events around each launch on
+ * the context stream) and clears the collected entries. */
+int nli_ctx_set_profiling(nli_ctx *ctx, int enable);
+/* Entry `index` (0-based, sorted by name) of the collected timings:
+ * kernel name, launches and total milliseconds.  NLI_E_INVALID past the end. */
+int nli_ctx_profile_entry(nli_ctx *ctx, int index, char *name, int name_len, int64_t *launches, double *ms);
+/* Running totals of this context: PatchMatch distance evaluations counted
+ * on the device, conjugate-gradient iterations (summed over channels) and
+ * the same weighted by the number of unknowns of each solve. */
+int nli_ctx_counters(nli_ctx *ctx, int64_t *candidates, int64_t *cg_iterations, int64_t *cg_unknown_iterations);
+
 /* ---- numeric helpers (L1) ------------------------------------------------ */
 /* GaussianWeights::calculate (gaussian_weights.cpp:19-79).  Host pointers:
  * writes size_x*size_y floats.  size_y == 1 gives the 1-D form used by the

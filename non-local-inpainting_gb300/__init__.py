@@ -89,6 +89,10 @@ def load(path=LIB_PATH):
     proto("nli_update", I, [P, up, P, P, P, P, P, P, I, I, I, ct.POINTER(ct.c_double)])
     proto("nli_process", I, [P, prp, P, P, I, I, I, P, st])
     proto("nli_process_device", I, [P, prp, P, P, I, I, I, P, st])
+    proto("nli_launch_count", ct.c_int64, [])
+    proto("nli_ctx_set_profiling", I, [P, I])
+    proto("nli_ctx_profile_entry", I, [P, I, ct.c_char_p, I, ct.POINTER(ct.c_int64), ct.POINTER(ct.c_double)])
+    proto("nli_ctx_counters", I, [P, ct.POINTER(ct.c_int64), ct.POINTER(ct.c_int64), ct.POINTER(ct.c_int64)])
     _lib = L
     return L
 
@@ -148,6 +152,28 @@ class Context:
 
     def synchronize(self):
         self._check(self.lib.nli_ctx_synchronize(self.h))
+
+    # -- observability
+    def launch_count(self):
+        return int(self.lib.nli_launch_count())
+
+    def set_profiling(self, enable):
+        self._check(self.lib.nli_ctx_set_profiling(self.h, 1 if enable else 0))
+
+    def profile(self):
+        """{kernel: (launches, total ms)} collected since set_profiling(True)."""
+        out, i = {}, 0
+        name = ct.create_string_buffer(64)
+        n, ms = ct.c_int64(), ct.c_double()
+        while self.lib.nli_ctx_profile_entry(self.h, i, name, 64, ct.byref(n), ct.byref(ms)) == 0:
+            out[name.value.decode()] = (n.value, ms.value)
+            i += 1
+        return out
+
+    def counters(self):
+        a, b, c = ct.c_int64(), ct.c_int64(), ct.c_int64()
+        self._check(self.lib.nli_ctx_counters(self.h, ct.byref(a), ct.byref(b), ct.byref(c)))
+        return {"candidates": a.value, "cg_iterations": b.value, "cg_unknown_iterations": c.value}
 
     # -- device tensors helpers
     def _f32(self, a):

@@ -1,8 +1,10 @@
 // The C ABI (include/nli.h): argument checking, context management and the
 // translation of internal errors into status codes.  Every entry point that
 // computes enqueues CUDA kernels; nothing here falls back to the CPU.
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <iterator>
 #include <new>
 
 #include "nli_device.cuh"
@@ -201,6 +203,46 @@ int nli_ctx_synchronize(nli_ctx *ctx)
 }
 
 const char *nli_last_error(nli_ctx *ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
+
+static std::atomic<long long> g_launches{0};
+
+void nli_count_launch_internal(void) { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+int64_t nli_launch_count(void) { return g_launches.load(); }
+
+int nli_ctx_set_profiling(nli_ctx *ctx, int enable)
+{
+	API_BEGIN(ctx)
+	ctx->settle_profile();
+	ctx->prof.clear();
+	ctx->profiling = enable != 0;
+	API_END(ctx)
+}
+
+int nli_ctx_profile_entry(nli_ctx *ctx, int index, char *name, int name_len, int64_t *launches, double *ms)
+{
+	API_BEGIN(ctx)
+	ctx->settle_profile();
+	NLI_REQUIRE(index >= 0 && index < (int)ctx->prof.size(), NLI_E_INVALID, "profile index out of range");
+	auto it = ctx->prof.begin();
+	std::advance(it, index);
+	if (name && name_len > 0) {
+		std::strncpy(name, it->first.c_str(), name_len - 1);
+		name[name_len - 1] = 0;
+	}
+	if (launches) *launches = it->second.launches;
+	if (ms) *ms = it->second.ms;
+	API_END(ctx)
+}
+
+int nli_ctx_counters(nli_ctx *ctx, int64_t *candidates, int64_t *cg_iterations, int64_t *cg_unknown_iterations)
+{
+	if (!ctx) return NLI_E_INVALID;
+	if (candidates) *candidates = ctx->candidates;
+	if (cg_iterations) *cg_iterations = ctx->cg_iterations;
+	if (cg_unknown_iterations) *cg_unknown_iterations = ctx->cg_unknown_iterations;
+	return NLI_OK;
+}
 
 int nli_gaussian_weights(int size_x, int size_y, float sigma_x, float sigma_y, float *host_out)
 {

@@ -6,13 +6,16 @@
 namespace nli {
 
 __global__ void k_distance_pairs(DistArgs a, const float *__restrict__ S, const float *__restrict__ GS, int sW,
-                                 const float *__restrict__ T, const float *__restrict__ GT, int tW,
+                                 int sH, const float *__restrict__ T, const float *__restrict__ GT, int tW, int tH,
                                  const int4 *__restrict__ pairs, int n, float *__restrict__ out)
 {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n) return;
 	const int4 q = pairs[i];
-	out[i] = dist_exact(a, S, GS, sW, T, GT, tW, q.x, q.y, q.z, q.w);
+	const bool inside = q.x >= a.rx && q.y >= a.ry && q.x + (a.px - a.rx) <= sW && q.y + (a.py - a.ry) <= sH &&
+	                    q.z >= a.rx && q.w >= a.ry && q.z + (a.px - a.rx) <= tW && q.w + (a.py - a.ry) <= tH;
+	// a patch leaving its image has no defined distance: NaN
+	out[i] = inside ? dist_exact(a, S, GS, sW, T, GT, tW, q.x, q.y, q.z, q.w) : __int_as_float(0x7fc00000);
 }
 
 // One block per target pixel; threads stride over the source pixels; the
@@ -103,7 +106,7 @@ extern "C" int nli_distance_pairs(nli_ctx *ctx, const nli_distance_params *dist,
 		if (n == 0) return NLI_OK;
 		const float *gs, *gt;
 		gradients_for(ctx, *dist, source, sW, sH, target, tW, tH, C, &gs, &gt);
-		k_distance_pairs<<<(n + 127) / 128, 128, 0, ctx->stream>>>(a, source, gs, sW, target, gt, tW,
+		k_distance_pairs<<<(n + 127) / 128, 128, 0, ctx->stream>>>(a, source, gs, sW, sH, target, gt, tW, tH,
 		                                                            reinterpret_cast<const int4 *>(pairs), n, out);
 		NLI_CHECK_LAUNCH();
 	} catch (const Error &e) {

@@ -30,7 +30,14 @@ struct Error {
 			                   std::string(#call) + ": " + cudaGetErrorString(e_)};        \
 	} while (0)
 
-#define NLI_CHECK_LAUNCH() NLI_CUDA(cudaGetLastError())
+// Every kernel launch of the library is followed by this check, which also
+// counts the launch (nli_launch_count).
+extern "C" void nli_count_launch_internal(void);
+#define NLI_CHECK_LAUNCH()                    \
+	do {                                      \
+		nli_count_launch_internal();          \
+		NLI_CUDA(cudaGetLastError());         \
+	} while (0)
 
 #define NLI_REQUIRE(cond, status, msg)                  \
 	do {                                                \
@@ -89,6 +96,42 @@ struct nli_ctx {
 	// running counters (for stats)
 	int64_t candidates = 0;
 	int64_t cg_iterations = 0;
+	int64_t cg_unknown_iterations = 0;  // sum over solves of iterations x unknowns
+	// optional per-region GPU timing with CUDA events (nli_ctx_set_profiling)
+	struct ProfEntry {
+		int64_t launches = 0;
+		double ms = 0.0;
+		std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+	};
+	bool profiling = false;
+	std::map<std::string, ProfEntry> prof;
+	std::vector<cudaEvent_t> event_pool;
+
+	cudaEvent_t take_event()
+	{
+		if (!event_pool.empty()) {
+			cudaEvent_t e = event_pool.back();
+			event_pool.pop_back();
+			return e;
+		}
+		cudaEvent_t e;
+		cudaEventCreate(&e);
+		return e;
+	}
+	void settle_profile()
+	{
+		cudaStreamSynchronize(stream);
+		for (auto &kv : prof) {
+			for (auto &pr : kv.second.pending) {
+				float ms = 0.f;
+				cudaEventElapsedTime(&ms, pr.first, pr.second);
+				kv.second.ms += ms;
+				event_pool.push_back(pr.first);
+				event_pool.push_back(pr.second);
+			}
+			kv.second.pending.clear();
+		}
+	}
 
 	template <class T>
 	T *buf(const std::string &name, size_t count)
@@ -98,6 +141,31 @@ struct nli_ctx {
 };
 
 namespace nli {
+
+// Times the kernels launched in its lifetime under `name` when the
+// context's profiling is on (events on the context stream).
+struct ProfScope {
+	nli_ctx *ctx;
+	const char *name;
+	cudaEvent_t a = nullptr;
+	ProfScope(nli_ctx *c, const char *n) : ctx(c), name(n)
+	{
+		if (ctx->profiling) {
+			a = ctx->take_event();
+			cudaEventRecord(a, ctx->stream);
+		}
+	}
+	~ProfScope()
+	{
+		if (a) {
+			cudaEvent_t b = ctx->take_event();
+			cudaEventRecord(b, ctx->stream);
+			auto &e = ctx->prof[name];
+			e.launches++;
+			e.pending.emplace_back(a, b);
+		}
+	}
+};
 
 // ------------------------------------------------------------ parameters
 constexpr int kMaxTaps = NLI_MAX_PATCH * NLI_MAX_PATCH;

@@ -26,11 +26,21 @@ struct PmArgs {
 	int sW, sH, tW, tH, nt;
 	int shots, max_window;
 	uint2 key;
+	// patch extent around a centre: [x - rx, x + ex) x [y - ry, y + ey)
+	int rx, ry, ex, ey;
 };
 
+// A source centre is usable when it is in the source mask and its whole
+// patch lies in the image (the masks of the inpainting driver guarantee the
+// latter through their margin; user masks may not).
 __device__ __forceinline__ bool src_ok(const PmArgs &p, int x, int y)
 {
-	return (unsigned)x < (unsigned)p.sW && (unsigned)y < (unsigned)p.sH && p.smask[y * p.sW + x];
+	return x >= p.rx && y >= p.ry && x + p.ex <= p.sW && y + p.ey <= p.sH && p.smask[y * p.sW + x];
+}
+
+__device__ __forceinline__ bool tgt_patch_inside(const PmArgs &p, int x, int y)
+{
+	return x >= p.rx && y >= p.ry && x + p.ex <= p.tW && y + p.ey <= p.tH;
 }
 
 __device__ __forceinline__ bool tgt_ok(const PmArgs &p, int x, int y)
@@ -75,7 +85,7 @@ __global__ void __launch_bounds__(128) k_pm_init(DistArgs a, PmArgs p, const int
 				tries++;
 			}
 		}
-		if (src_ok(p, n.x, n.y)) {
+		if (src_ok(p, n.x, n.y) && tgt_patch_inside(p, x, y)) {
 			nnf[pix] = n;
 			dist[pix] = dist_fast<KIND, C, NF4>(a, p.fs, p.sW, p.ft, p.tW, n.x, n.y, x, y);
 			evals = 1;
@@ -100,9 +110,14 @@ __global__ void __launch_bounds__(128) k_pm_sweep(DistArgs a, PmArgs p, int swee
 		const int x = pix % p.tW, y = pix / p.tW;
 		int2 best = nnf_in[pix];
 		float bd = dist_in[pix];
+		const bool inside = tgt_patch_inside(p, x, y);
+		if (!inside) {
+			best = make_int2(-1, -1);
+			bd = FLT_MAX;
+		}
 
 		auto consider = [&](int cx, int cy) {
-			if ((cx != best.x || cy != best.y) && src_ok(p, cx, cy)) {
+			if (inside && (cx != best.x || cy != best.y) && src_ok(p, cx, cy)) {
 				const float d = dist_fast<KIND, C, NF4>(a, p.fs, p.sW, p.ft, p.tW, cx, cy, x, y);
 				evals++;
 				if (d < bd) {
@@ -205,10 +220,14 @@ static void run_sweeps(nli_ctx *ctx, const DistArgs &a, const PmArgs &p, int ite
                        int2 *nnf_x, float *dist_x, int2 *nnf_y, float *dist_y, unsigned long long *counter)
 {
 	const int block = 128, grid = (p.nt + block - 1) / block;
-	k_pm_init<KIND, C, NF4><<<grid, block, 0, ctx->stream>>>(a, p, init, nnf_x, dist_x, counter);
-	NLI_CHECK_LAUNCH();
+	{
+		ProfScope ps(ctx, "pm_init");
+		k_pm_init<KIND, C, NF4><<<grid, block, 0, ctx->stream>>>(a, p, init, nnf_x, dist_x, counter);
+		NLI_CHECK_LAUNCH();
+	}
 	for (int it = 0; it < iterations; it++) {
 		const bool even = (it % 2) == 0;
+		ProfScope ps(ctx, "pm_sweep");
 		k_pm_sweep<KIND, C, NF4><<<grid, block, 0, ctx->stream>>>(
 		    a, p, it, jump_for(it, p.tW, p.tH), even ? nnf_x : nnf_y, even ? dist_x : dist_y, even ? nnf_y : nnf_x,
 		    even ? dist_y : dist_x, counter);
@@ -270,6 +289,10 @@ void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patch
 		p.nt = n_target;
 		p.shots = pm.random_shots;
 		p.max_window = (pm.window != -1) ? pm.window : max(sW, sH);
+		p.rx = a.rx;
+		p.ry = a.ry;
+		p.ex = a.px - a.rx;
+		p.ey = a.py - a.ry;
 		const uint64_t call = ctx->call_counter++;
 		const uint64_t k = ctx->seed ^ (call * 0x9E3779B97F4A7C15ULL);
 		p.key = make_uint2((uint32_t)k, (uint32_t)(k >> 32) ^ (uint32_t)call);

@@ -528,7 +528,7 @@ __global__ void k_fill_int(int32_t *p, int n, int v)
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = v;
 }
 
-static double read_total(nli_ctx *ctx, double *partials, int n, int *cg_iters_dev, int C)
+static double read_total(nli_ctx *ctx, double *partials, int n, int *cg_iters_dev, int C, int nh = 0)
 {
 	launch_sum_partials(ctx->stream, partials, n, partials + n);
 	char *h = static_cast<char *>(ctx->host_pinned);
@@ -538,7 +538,10 @@ static double read_total(nli_ctx *ctx, double *partials, int n, int *cg_iters_de
 	NLI_CUDA(cudaStreamSynchronize(ctx->stream));
 	if (cg_iters_dev) {
 		const int *it = reinterpret_cast<const int *>(h + 64);
-		for (int c = 0; c < C; c++) ctx->cg_iterations += it[c];
+		for (int c = 0; c < C; c++) {
+			ctx->cg_iterations += it[c];
+			ctx->cg_unknown_iterations += (int64_t)it[c] * nh;
+		}
 	}
 	return *reinterpret_cast<double *>(h);
 }
@@ -558,9 +561,12 @@ static void poisson_run(nli_ctx *ctx, const UpdArgs &u, const nli_update_params 
 	co.U = ctx->buf<float>("poi.U", n * C);
 	co.GX = ctx->buf<float>("poi.GX", n * C);
 	co.GY = ctx->buf<float>("poi.GY", n * C);
+	{
+	ProfScope ps(ctx, "poisson_coef");
 	k_poisson_coef<<<(nh + 127) / 128, 128, 0, s>>>(u, hole, nh, dom, ext, nnf, conf, image,
 	                                                 reinterpret_cast<const float2 *>(grad), co);
 	NLI_CHECK_LAUNCH();
+	}
 	PoissonArgs pa;
 	pa.W = W;
 	pa.H = H;
@@ -576,8 +582,11 @@ static void poisson_run(nli_ctx *ctx, const UpdArgs &u, const nli_update_params 
 	float *r = ctx->buf<float>("poi.r", (size_t)nh * C);
 	float *d = ctx->buf<float>("poi.d", (size_t)nh * C);
 	float *q = ctx->buf<float>("poi.q", (size_t)nh * C);
-	k_poisson_setup<<<(nh + 255) / 256, 256, 0, s>>>(pa, hole, hole_index, co, image, orig, unk, b, x);
-	NLI_CHECK_LAUNCH();
+	{
+		ProfScope ps(ctx, "poisson_setup");
+		k_poisson_setup<<<(nh + 255) / 256, 256, 0, s>>>(pa, hole, hole_index, co, image, orig, unk, b, x);
+		NLI_CHECK_LAUNCH();
+	}
 
 	int dev_blocks_per_sm = 0;
 	NLI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&dev_blocks_per_sm, k_poisson_cg, kCgBlock, 0));
@@ -592,7 +601,11 @@ static void poisson_run(nli_ctx *ctx, const UpdArgs &u, const nli_update_params 
 	DevStatus *st = ctx->status;
 	const float *orig_c = orig;
 	void *args[] = {&pa, &unk, &b, &x, &r, &d, &q, &part, &st, &iters, (void *)&hole, &orig_c, &image, &diff_part};
-	NLI_CUDA(cudaLaunchCooperativeKernel((const void *)k_poisson_cg, dim3(grid), dim3(kCgBlock), args, 0, s));
+	{
+		ProfScope ps(ctx, "poisson_cg");
+		NLI_CUDA(cudaLaunchCooperativeKernel((const void *)k_poisson_cg, dim3(grid), dim3(kCgBlock), args, 0, s));
+		nli_count_launch_internal();
+	}
 	*n_partials = grid;
 	(void)partials_out;
 }
@@ -628,7 +641,7 @@ double update_run(nli_ctx *ctx, const nli_update_params &up, float *image, const
 			launch_sum_partials(s, diff_part, np, diff_part + np);
 			return 0.0;
 		}
-		const double t = read_total(ctx, diff_part, np, ctx->buf<int>("poi.iters", 4), C);
+		const double t = read_total(ctx, diff_part, np, ctx->buf<int>("poi.iters", 4), C, nh);
 		int *hs = static_cast<int *>(ctx->host_pinned) + 128;
 		NLI_CUDA(cudaMemcpy(hs, &ctx->status->timeout, sizeof(int), cudaMemcpyDeviceToHost));
 		NLI_REQUIRE(*hs == 0, NLI_E_TIMEOUT, "conjugate gradient grid barrier timed out");
@@ -640,10 +653,12 @@ double update_run(nli_ctx *ctx, const nli_update_params &up, float *image, const
 	if (up.method == NLI_UPDATE_MEANS) {
 		grid = (nh + 255) / 256;
 		partials = ctx->buf<double>("upd.partials", grid + 1);
+		ProfScope ps(ctx, "nlmeans");
 		k_nlmeans<<<grid, 256, 0, s>>>(u, image, hole, nh, dom, nnf, conf, newval, partials);
 	} else {
 		grid = (nh + kMedWarps - 1) / kMedWarps;
 		partials = ctx->buf<double>("upd.partials", grid + 1);
+		ProfScope ps(ctx, "nlmedians");
 		k_nlmedians<<<grid, 32 * kMedWarps, 0, s>>>(u, image, hole, nh, dom, nnf, conf, newval, partials);
 	}
 	NLI_CHECK_LAUNCH();
