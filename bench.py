@@ -346,14 +346,43 @@ def run_ours(args):
     return 0
 
 
+def run_case(args):
+    """Small single-kernel cases for profiler captures: one PatchMatch call
+    (init + 10 sweeps) or one NL-Poisson update on the finest scale of the
+    benchmark workload, with the masks the driver builds there."""
+    import torch
+    pkg = ge.package()
+    ctx = pkg.Context(0)
+    ctx.set_seed(7)
+    img, mask, p = workload()
+    ext = ctx.extended_domain(mask, p.update.patch_x, p.update.patch_y)
+    src, tgt, _ = ctx.scale_masks(ext, p.update.patch_x // 2, True)
+    d_img = ctx._f32(img)
+    d_img[torch.from_numpy(mask).to(d_img.device).bool()] = 128.0
+    nnf = None
+    for _ in range(args.steps):
+        nnf, _, e = ctx.patchmatch(p.distance, p.patchmatch, d_img, src, d_img, tgt, init=nnf)
+    if args.case == "update":
+        conf = ctx.confidence_mask(mask, p.conf_decay_time, p.conf_asymptotic)
+        for _ in range(args.steps):
+            out, tot = ctx.update(p.update, d_img, d_img, mask, ext, nnf, conf)
+    torch.cuda.synchronize()
+    print(json.dumps({"case": args.case, "energy": e, "counters": ctx.counters()}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--case", default=None, choices=["patchmatch", "update"],
+                    help="run one small profiling case instead of the benchmark")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
+    if args.case:
+        return run_case(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)

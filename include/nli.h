@@ -161,9 +161,12 @@ int nli_ctx_set_profiling(nli_ctx *ctx, int enable);
  * kernel name, launches and total milliseconds.  NLI_E_INVALID past the end. */
 int nli_ctx_profile_entry(nli_ctx *ctx, int index, char *name, int name_len, int64_t *launches, double *ms);
 /* Running totals of this context: PatchMatch distance evaluations counted
- * on the device, conjugate-gradient iterations (summed over channels) and
- * the same weighted by the number of unknowns of each solve. */
-int nli_ctx_counters(nli_ctx *ctx, int64_t *candidates, int64_t *cg_iterations, int64_t *cg_unknown_iterations);
+ * on the device, the part of them stopped early (after the first 32 taps
+ * their partial sum already exceeded the current match), conjugate-gradient
+ * iterations (summed over channels) and the same weighted by the number of
+ * unknowns of each solve.  Any pointer may be NULL. */
+int nli_ctx_counters(nli_ctx *ctx, int64_t *candidates, int64_t *candidates_partial, int64_t *cg_iterations,
+                     int64_t *cg_unknown_iterations);
 
 /* ---- numeric helpers (L1) ------------------------------------------------ */
 /* GaussianWeights::calculate (gaussian_weights.cpp:19-79).  Host pointers:

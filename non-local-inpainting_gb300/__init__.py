@@ -92,7 +92,8 @@ def load(path=LIB_PATH):
     proto("nli_launch_count", ct.c_int64, [])
     proto("nli_ctx_set_profiling", I, [P, I])
     proto("nli_ctx_profile_entry", I, [P, I, ct.c_char_p, I, ct.POINTER(ct.c_int64), ct.POINTER(ct.c_double)])
-    proto("nli_ctx_counters", I, [P, ct.POINTER(ct.c_int64), ct.POINTER(ct.c_int64), ct.POINTER(ct.c_int64)])
+    proto("nli_ctx_counters", I, [P, ct.POINTER(ct.c_int64), ct.POINTER(ct.c_int64), ct.POINTER(ct.c_int64),
+                                  ct.POINTER(ct.c_int64)])
     _lib = L
     return L
 
@@ -171,9 +172,10 @@ class Context:
         return out
 
     def counters(self):
-        a, b, c = ct.c_int64(), ct.c_int64(), ct.c_int64()
-        self._check(self.lib.nli_ctx_counters(self.h, ct.byref(a), ct.byref(b), ct.byref(c)))
-        return {"candidates": a.value, "cg_iterations": b.value, "cg_unknown_iterations": c.value}
+        a, p, b, c = ct.c_int64(), ct.c_int64(), ct.c_int64(), ct.c_int64()
+        self._check(self.lib.nli_ctx_counters(self.h, ct.byref(a), ct.byref(p), ct.byref(b), ct.byref(c)))
+        return {"candidates": a.value, "candidates_partial": p.value, "cg_iterations": b.value,
+                "cg_unknown_iterations": c.value}
 
     # -- device tensors helpers
     def _f32(self, a):

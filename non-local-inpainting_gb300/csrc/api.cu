@@ -52,12 +52,6 @@ std::vector<float> gaussian_weights_host(unsigned sx, unsigned sy, float sigma_x
 	return w;
 }
 
-int feature_float4s(int kind, int C)
-{
-	int comps = (kind == NLI_DIST_L2_COMBINED || kind == NLI_DIST_L2_RGBD) ? 3 * C : C;
-	return (comps + 3) / 4;
-}
-
 void fill_dist_args(DistArgs &a, const nli_distance_params &p, int C)
 {
 	NLI_REQUIRE(p.patch_x >= 1 && p.patch_y >= 1 && p.patch_x <= NLI_MAX_PATCH && p.patch_y <= NLI_MAX_PATCH,
@@ -73,7 +67,7 @@ void fill_dist_args(DistArgs &a, const nli_distance_params &p, int C)
 	a.rx = p.patch_x / 2;
 	a.ry = p.patch_y / 2;
 	a.C = C;
-	a.nf4 = feature_float4s(p.kind, C);
+	feature_layout(p.kind, C, &a.p4, &a.f1);
 	a.lambda = p.lambda;
 	a.lambda_d = p.lambda_d;
 	std::vector<float> w = gaussian_weights_host(p.patch_x, p.patch_y, p.sigma, p.sigma);
@@ -235,10 +229,12 @@ int nli_ctx_profile_entry(nli_ctx *ctx, int index, char *name, int name_len, int
 	API_END(ctx)
 }
 
-int nli_ctx_counters(nli_ctx *ctx, int64_t *candidates, int64_t *cg_iterations, int64_t *cg_unknown_iterations)
+int nli_ctx_counters(nli_ctx *ctx, int64_t *candidates, int64_t *candidates_partial, int64_t *cg_iterations,
+                     int64_t *cg_unknown_iterations)
 {
 	if (!ctx) return NLI_E_INVALID;
 	if (candidates) *candidates = ctx->candidates;
+	if (candidates_partial) *candidates_partial = ctx->candidates_partial;
 	if (cg_iterations) *cg_iterations = ctx->cg_iterations;
 	if (cg_unknown_iterations) *cg_unknown_iterations = ctx->cg_unknown_iterations;
 	return NLI_OK;

@@ -28,11 +28,22 @@ void launch_gradient(cudaStream_t s, const float *img, int W, int H, int C, floa
 	NLI_CHECK_LAUNCH();
 }
 
-// Packed features: [u_0..u_{C-1}, gx_0, gy_0, ..., gx_{C-1}, gy_{C-1}] with
-// zero padding to nf4 float4 (gradient kinds), or [u_0..u_{C-1}] padded
-// (colour-only kinds).  One thread per pixel.
+// Features read by the PatchMatch distance, plane-major: per pixel the
+// components [u_0..u_{C-1}, gx_0, gy_0, ..., gx_{C-1}, gy_{C-1}] (gradient
+// kinds) or [u_0..u_{C-1}] (colour-only kinds); components 4j..4j+3 go to
+// float4 plane j (p4 planes of W*H float4), a ninth component (C = 3
+// gradient kinds: 9 components, 36 bytes per pixel) to one float plane.
+// Missing components of the last float4 are zero.
+void feature_layout(int kind, int C, int *p4, int *f1)
+{
+	const int comps = (kind == NLI_DIST_L2_COMBINED || kind == NLI_DIST_L2_RGBD) ? 3 * C : C;
+	*f1 = (comps % 4 == 1 && comps > 1) ? 1 : 0;
+	*p4 = (comps - *f1 + 3) / 4;
+}
+
 template <bool GRAD>
-__global__ void k_features(const float *__restrict__ img, int W, int H, int C, int nf4, float4 *__restrict__ feat)
+__global__ void k_features(const float *__restrict__ img, int W, int H, int C, int p4, int f1,
+                           float4 *__restrict__ planes4, float *__restrict__ plane1)
 {
 	const int n = W * H;
 	for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
@@ -49,20 +60,22 @@ __global__ void k_features(const float *__restrict__ img, int W, int H, int C, i
 				f[C + 2 * c + 1] = (y == H - 1) ? 0.0f : __fsub_rn(u[(size_t)C * W + c], v);
 			}
 		}
-		float4 *o = feat + (size_t)p * nf4;
-		for (int k = 0; k < nf4; k++) o[k] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);
+		for (int k = 0; k < p4; k++)
+			planes4[(size_t)k * n + p] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);
+		if (f1) plane1[p] = f[4 * p4];
 	}
 }
 
-void launch_features(cudaStream_t s, int kind, const float *img, int W, int H, int C, float4 *feat)
+void launch_features(cudaStream_t s, int kind, const float *img, int W, int H, int C, float4 *planes4, float *plane1)
 {
 	const int n = W * H;
 	const int block = 256, grid = (n + block - 1) / block;
-	const int nf4 = feature_float4s(kind, C);
+	int p4, f1;
+	feature_layout(kind, C, &p4, &f1);
 	if (kind == NLI_DIST_L2_COMBINED || kind == NLI_DIST_L2_RGBD)
-		k_features<true><<<grid, block, 0, s>>>(img, W, H, C, nf4, feat);
+		k_features<true><<<grid, block, 0, s>>>(img, W, H, C, p4, f1, planes4, plane1);
 	else
-		k_features<false><<<grid, block, 0, s>>>(img, W, H, C, nf4, feat);
+		k_features<false><<<grid, block, 0, s>>>(img, W, H, C, p4, f1, planes4, plane1);
 	NLI_CHECK_LAUNCH();
 }
 

@@ -55,8 +55,10 @@ struct Rng {
 		used++;
 		return r;
 	}
-	// draw in [0, n), n >= 1 (the reference uses rand() % n)
-	__device__ __forceinline__ int below(int n) { return (int)(next() % (uint32_t)n); }
+	// draw in [0, n), n >= 1, by the multiply-high range reduction of
+	// D. Lemire, "Fast random integer generation in an interval" (2019)
+	// (the reference draws rand() % n)
+	__device__ __forceinline__ int below(int n) { return (int)__umulhi(next(), (uint32_t)n); }
 };
 
 // ------------------------------------------------------------------------
@@ -158,72 +160,6 @@ __device__ inline float dist_exact(const DistArgs &a, const float *__restrict__ 
 			D = fa(D, fm(w, norm));
 		}
 	return __fdiv_rn(D, (float)((unsigned)a.px * (unsigned)a.py));
-}
-
-// ------------------------------------------------------------------------
-// Patch distances, fast single-precision variant used inside PatchMatch.
-// Reads the packed feature image (NF4 float4 per pixel, see
-// launch_features) and accumulates in float with fused multiply-adds.  Its
-// relative deviation from the reference-exact value is ~1e-6.
-template <int KIND, int C, int NF4>
-__device__ __forceinline__ float dist_fast(const DistArgs &a, const float4 *__restrict__ fsrc, int sW,
-                                           const float4 *__restrict__ ftgt, int tW, int sx, int sy, int tx,
-                                           int ty)
-{
-	float D = 0.f, G = 0.f, Dd = 0.f, Gd = 0.f;
-	const float *pw = a.weights;
-	for (int dy = -a.ry; dy < a.py - a.ry; dy++) {
-		const float4 *sp = fsrc + ((size_t)(sy + dy) * sW + (sx - a.rx)) * NF4;
-		const float4 *tp = ftgt + ((size_t)(ty + dy) * tW + (tx - a.rx)) * NF4;
-#pragma unroll 3
-		for (int dx = 0; dx < a.px; dx++, ++pw) {
-			float f[4 * NF4];
-#pragma unroll
-			for (int k = 0; k < NF4; k++) {
-				float4 s4 = __ldg(sp + dx * NF4 + k);
-				float4 t4 = __ldg(tp + dx * NF4 + k);
-				f[4 * k + 0] = s4.x - t4.x;
-				f[4 * k + 1] = s4.y - t4.y;
-				f[4 * k + 2] = s4.z - t4.z;
-				f[4 * k + 3] = s4.w - t4.w;
-			}
-			const float w = *pw;
-			if (KIND == NLI_DIST_L1_NORM) {
-				float n = 0.f;
-#pragma unroll
-				for (int c = 0; c < C; c++) n += fabsf(f[c]);
-				D = fmaf(w, n, D);
-			} else if (KIND == NLI_DIST_L2_NORM) {
-				float n = 0.f;
-#pragma unroll
-				for (int c = 0; c < C; c++) n = fmaf(f[c], f[c], n);
-				D = fmaf(w, n, D);
-			} else if (KIND == NLI_DIST_L2_RGBD) {
-				float n = 0.f, g = 0.f;
-#pragma unroll
-				for (int c = 0; c < 3; c++) n = fmaf(f[c], f[c], n);
-#pragma unroll
-				for (int c = 0; c < 6; c++) g = fmaf(f[4 + c], f[4 + c], g);
-				D = fmaf(w, n, D);
-				G = fmaf(w, g, G);
-				Dd = fmaf(w, f[3] * f[3], Dd);
-				Gd = fmaf(w, fmaf(f[10], f[10], f[11] * f[11]), Gd);
-			} else {
-				float n = 0.f, g = 0.f;
-#pragma unroll
-				for (int c = 0; c < C; c++) n = fmaf(f[c], f[c], n);
-#pragma unroll
-				for (int c = 0; c < 2 * C; c++) g = fmaf(f[C + c], f[C + c], g);
-				D = fmaf(w, n, D);
-				G = fmaf(w, g, G);
-			}
-		}
-	}
-	const float invP = 1.0f / (float)(a.px * a.py);
-	if (KIND == NLI_DIST_L1_NORM || KIND == NLI_DIST_L2_NORM) return D * invP;
-	float r = a.lambda * D + (1.0f - a.lambda) * G;
-	if (KIND == NLI_DIST_L2_RGBD) r += a.lambda_d * Dd + (1.0f - a.lambda_d) * Gd;
-	return r * invP;
 }
 
 // ------------------------------------------------------------------------

@@ -88,6 +88,7 @@ struct nli_ctx {
 	uint64_t call_counter = 0;
 	std::string last_error;
 	int num_sms = 0;
+	int cg_cluster_max = -1;  // largest thread-block cluster for the CG kernel (queried once)
 	std::map<std::string, nli::DevBuf> bufs;
 	// pinned host staging for small results
 	void *host_pinned = nullptr;
@@ -95,6 +96,7 @@ struct nli_ctx {
 	nli::DevStatus *status = nullptr;
 	// running counters (for stats)
 	int64_t candidates = 0;
+	int64_t candidates_partial = 0;  // candidates rejected after the first 32 taps
 	int64_t cg_iterations = 0;
 	int64_t cg_unknown_iterations = 0;  // sum over solves of iterations x unknowns
 	// optional per-region GPU timing with CUDA events (nli_ctx_set_profiling)
@@ -175,7 +177,7 @@ struct DistArgs {
 	int kind;
 	int px, py, rx, ry;  // patch size and radius (radius = size / 2)
 	int C;               // image channels
-	int nf4;             // float4 per pixel in the feature image
+	int p4, f1;          // feature planes: float4 planes and float planes (see feature_layout)
 	float lambda, lambda_d;
 	float weights[kMaxTaps];  // Gaussian patch weights, row-major
 };
@@ -183,15 +185,13 @@ struct DistArgs {
 // ---------------------------------------------------------- host helpers
 std::vector<float> gaussian_weights_host(unsigned sx, unsigned sy, float sigma_x, float sigma_y);
 void fill_dist_args(DistArgs &a, const nli_distance_params &p, int C);
-int feature_float4s(int kind, int C);
+void feature_layout(int kind, int C, int *p4, int *f1);
 
 // ------------------------------------------------------------- launchers
 // gradient.cu
 void launch_gradient(cudaStream_t s, const float *img, int W, int H, int C, float *grad);
-// Feature image for the distances: per pixel nf4 float4 =
-// [u_0..u_{C-1}, gx_0, gy_0, ..., gx_{C-1}, gy_{C-1}, 0-padding] (colour only
-// for the L2Norm/L1Norm kinds).
-void launch_features(cudaStream_t s, int kind, const float *img, int W, int H, int C, float4 *feat);
+// Plane-major feature image of the PatchMatch distance (gradient.cu).
+void launch_features(cudaStream_t s, int kind, const float *img, int W, int H, int C, float4 *planes4, float *plane1);
 
 // compact.cu: raster-order list of the pixels with mask != 0; returns count
 int compact_mask(nli_ctx *ctx, const uint8_t *mask, int W, int H, int32_t *list, const char *tag);

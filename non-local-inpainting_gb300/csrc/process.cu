@@ -241,8 +241,8 @@ struct Driver {
 			}
 		}
 		const int64_t cand0 = ctx->candidates, cg0 = ctx->cg_iterations;
-		unsigned long long *counter = ctx->buf<unsigned long long>("pm.counter", 1);
-		NLI_CUDA(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), ctx->stream));
+		unsigned long long *counter = ctx->buf<unsigned long long>("pm.counter", 2);
+		NLI_CUDA(cudaMemsetAsync(counter, 0, 2 * sizeof(unsigned long long), ctx->stream));
 		cudaStream_t s = ctx->stream;
 		NLI_CUDA(cudaMemcpyAsync(lv[0].img, img, (size_t)W * H * C * sizeof(float), cudaMemcpyDeviceToDevice, s));
 		NLI_CUDA(cudaMemcpyAsync(lv[0].mask, mask, (size_t)W * H, cudaMemcpyDeviceToDevice, s));
@@ -275,9 +275,10 @@ struct Driver {
 		}
 		NLI_CUDA(cudaMemcpyAsync(out, lv[0].img, (size_t)W * H * C * sizeof(float), cudaMemcpyDeviceToDevice, s));
 		unsigned long long *hc = reinterpret_cast<unsigned long long *>(ctx->host_pinned);
-		NLI_CUDA(cudaMemcpyAsync(hc, counter, sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+		NLI_CUDA(cudaMemcpyAsync(hc, counter, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
 		NLI_CUDA(cudaStreamSynchronize(s));
 		ctx->candidates = cand0 + (int64_t)hc[0];
+		ctx->candidates_partial += (int64_t)hc[1];
 		if (stats) {
 			stats->patchmatch_calls = pm_calls;
 			stats->update_calls = upd_calls;

@@ -287,6 +287,10 @@ struct Unknown {
 	float S;         // unscaled a1 / a2 at the centre
 	float s_up, s_left, s_down, s_right;  // unscaled link coefficients (0 if no link)
 	int n_up, n_left, n_down, n_right;    // unknown index of the neighbour, -1 if not a hole pixel
+	// the same neighbours as (owning CTA << 20) | index within its range,
+	// for the cluster kernel (-1 if not a hole pixel)
+	int c_up, c_left, c_down, c_right;
+	int links;  // bit 0: down link inside the image, bit 1: right link inside the image
 };
 
 struct PoissonArgs {
@@ -298,9 +302,10 @@ struct PoissonArgs {
 
 // Right-hand side b and initial perturbation delta0 = image - orig
 // (patch_non_local_poisson.cpp:62-82), and the per-unknown system data.
-__global__ void k_poisson_setup(PoissonArgs a, const int32_t *__restrict__ hole, const int32_t *__restrict__ hole_index,
-                                CoefOut co, const float *__restrict__ img, const float *__restrict__ orig,
-                                Unknown *__restrict__ unk, float *__restrict__ b, float *__restrict__ x0)
+__global__ void k_poisson_setup(PoissonArgs a, int chunk, const int32_t *__restrict__ hole,
+                                const int32_t *__restrict__ hole_index, CoefOut co, const float *__restrict__ img,
+                                const float *__restrict__ orig, Unknown *__restrict__ unk, float *__restrict__ b,
+                                float *__restrict__ x0)
 {
 	const int k = blockIdx.x * blockDim.x + threadIdx.x;
 	if (k >= a.nh) return;
@@ -317,6 +322,12 @@ __global__ void k_poisson_setup(PoissonArgs a, const int32_t *__restrict__ hole,
 	n.n_left = (x != 0) ? hole_index[pix - 1] : -1;
 	n.n_down = (y != H - 1) ? hole_index[pix + W] : -1;
 	n.n_right = (x != W - 1) ? hole_index[pix + 1] : -1;
+	auto code = [chunk](int m) { return (m >= 0 && chunk > 0) ? ((m / chunk) << 20) | (m % chunk) : -1; };
+	n.c_up = code(n.n_up);
+	n.c_left = code(n.n_left);
+	n.c_down = code(n.n_down);
+	n.c_right = code(n.n_right);
+	n.links = ((y != H - 1) ? 1 : 0) | ((x != W - 1) ? 2 : 0);
 	unk[k] = n;
 	for (int c = 0; c < C; c++) {
 		const float lam = a.lambda[c], oml = 1.0f - lam;
@@ -517,6 +528,274 @@ __global__ void __launch_bounds__(kCgBlock) k_poisson_cg(PoissonArgs a, const Un
 	if (threadIdx.x == 0) diff_part[blockIdx.x] = dacc;
 }
 
+// Conjugate gradient on one thread-block cluster with every vector and the
+// system itself in shared memory.
+//
+// CTA `rank` of the cluster (up to 16 CTAs of 512 threads) owns the
+// contiguous unknown range [rank * chunk, (rank + 1) * chunk), chunk <=
+// 4096, and keeps in its shared memory the residual r, two alternating
+// direction buffers, the solution x and a compact 24-byte record per
+// unknown (its coefficients and 16-bit neighbour codes: owning CTA << 12 |
+// index); q = A d stays in registers.  Neighbours owned by another CTA are
+// read through distributed shared memory.  Iteration (as the reference's
+// conjugte_gradient, patch_non_local_poisson.cpp:387-477, with the
+// residual updated by recurrence): d = r + beta d_old (folded into the
+// stencil phase, formed at the neighbours from r and d_old), q = A d,
+// alpha = |r|^2 / <r, q>, x += alpha d, r -= alpha q, beta = |r'|^2 / |r|^2.
+// Two cluster barriers per iteration; block partial sums are exchanged
+// through distributed shared memory and added in rank order by one warp,
+// so every CTA holds the same totals.  alpha and beta are formed once per
+// CTA in double precision.
+constexpr int kClusterBlock = 512;
+constexpr int kClusterMax = 16;
+constexpr int kClusterMaxChunk = 4096;
+constexpr int kClusterPerThread = kClusterMaxChunk / kClusterBlock;  // unknowns per thread
+constexpr int kClusterVectors = 4;  // r, d (twice), x
+constexpr int kNoNb = 0xFFFF;
+
+struct UnkC {
+	float S, s_up, s_left;
+	uint32_t ud;     // up code << 16 | down code
+	uint32_t lr;     // left code << 16 | right code
+	uint32_t links;  // bit 0: down link inside the image, bit 1: right link inside the image
+};
+
+__global__ void k_poisson_compact(const Unknown *__restrict__ unk, int nh, int chunk, UnkC *__restrict__ out)
+{
+	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= nh) return;
+	const Unknown n = unk[k];
+	auto code = [chunk](int m) -> uint32_t {
+		return (m >= 0) ? (uint32_t)(((m / chunk) << 12) | (m % chunk)) : (uint32_t)kNoNb;
+	};
+	UnkC c;
+	c.S = n.S;
+	c.s_up = n.s_up;
+	c.s_left = n.s_left;
+	c.ud = (code(n.n_up) << 16) | code(n.n_down);
+	c.lr = (code(n.n_left) << 16) | code(n.n_right);
+	c.links = (uint32_t)n.links;
+	out[k] = c;
+}
+
+template <int C>
+__global__ void __launch_bounds__(kClusterBlock, 1)
+    k_poisson_cg_cluster(PoissonArgs a, int chunk, const UnkC *__restrict__ unk_g, const float *__restrict__ b,
+                         const float *__restrict__ x0, int *__restrict__ iters_out, const int32_t *__restrict__ hole,
+                         const float *orig, float *img, double *__restrict__ diff_part)
+{
+	namespace cgs = cooperative_groups;
+	cgs::cluster_group cluster = cgs::this_cluster();
+	extern __shared__ float smem[];
+	__shared__ double red[kClusterBlock / 32][4];
+	__shared__ double partA[4], partB[4], tot[4];
+	__shared__ float s_coef[4];
+	__shared__ int s_active[4];
+	__shared__ float *base[3][kClusterMax];  // r, dA, dB of every CTA
+	const int rank = (int)cluster.block_rank(), ncta = (int)cluster.num_blocks();
+	const int nh = a.nh;
+	const int lo = rank * chunk, own = max(0, min(nh, lo + chunk) - lo);
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	const size_t vlen = (size_t)C * chunk;
+	float *s_r = smem, *s_dA = smem + vlen, *s_dB = smem + 2 * vlen, *s_x = smem + 3 * vlen;
+	UnkC *s_unk = reinterpret_cast<UnkC *>(smem + kClusterVectors * vlen);
+	if (threadIdx.x < ncta) {
+		base[0][threadIdx.x] = cluster.map_shared_rank(s_r, (int)threadIdx.x);
+		base[1][threadIdx.x] = cluster.map_shared_rank(s_dA, (int)threadIdx.x);
+		base[2][threadIdx.x] = cluster.map_shared_rank(s_dB, (int)threadIdx.x);
+	}
+	for (int l = threadIdx.x; l < own; l += blockDim.x) s_unk[l] = unk_g[lo + l];
+	__syncthreads();
+
+	auto block_reduce = [&](const float *v, double *dst) {
+#pragma unroll
+		for (int c = 0; c < C; c++) {
+			const float s = warp_sum(v[c]);
+			if (lane == 0) red[wid][c] = (double)s;
+		}
+		__syncthreads();
+		if (threadIdx.x < C) {
+			double s = 0.0;
+			for (int w = 0; w < kClusterBlock / 32; w++) s += red[w][threadIdx.x];
+			dst[threadIdx.x] = s;
+		}
+	};
+	auto cluster_total = [&](double *src, double *out) {
+		if (wid == 0) {
+#pragma unroll
+			for (int c = 0; c < C; c++) {
+				double v = (lane < ncta) ? cluster.map_shared_rank(src, lane)[c] : 0.0;
+				v = warp_sum(v);
+				if (lane == 0) tot[c] = v;
+			}
+		}
+		__syncthreads();
+#pragma unroll
+		for (int c = 0; c < C; c++) out[c] = tot[c];
+		__syncthreads();
+	};
+	// channel values of vector `v` (0: r, 1: dA, 2: dB) at a 16-bit code
+	auto nb = [&](int v, uint32_t code) -> const float * {
+		const int o = (int)(code >> 12), l = (int)(code & 0xFFF);
+		const float *bp = (o == rank) ? (v == 0 ? s_r : v == 1 ? s_dA : s_dB) : base[v][o];
+		return bp + (size_t)l * C;
+	};
+
+	// r0 = b - A x0 (x0 from global: neighbours may belong to other CTAs)
+	float facc[4];
+#pragma unroll
+	for (int c = 0; c < 4; c++) facc[c] = 0.f;
+	for (int l = threadIdx.x; l < own; l += blockDim.x) {
+		const int k = lo + l;
+		const UnkC n = s_unk[l];
+		const uint32_t codes[4] = {n.ud >> 16, n.lr >> 16, n.ud & 0xFFFF, n.lr & 0xFFFF};
+		const float coefs[4] = {n.s_up, n.s_left, (n.links & 1) ? n.S : 0.f, (n.links & 2) ? n.S : 0.f};
+		const float sum = coefs[0] + coefs[1] + coefs[2] + coefs[3];
+		int gk[4];
+#pragma unroll
+		for (int j = 0; j < 4; j++)
+			gk[j] = (codes[j] != kNoNb) ? (int)(codes[j] >> 12) * chunk + (int)(codes[j] & 0xFFF) : -1;
+#pragma unroll
+		for (int c = 0; c < C; c++) {
+			const float *xc = x0 + (size_t)c * nh;
+			const float xk = xc[k];
+			float lap = -xk * sum;
+#pragma unroll
+			for (int j = 0; j < 4; j++)
+				if (gk[j] >= 0) lap += coefs[j] * xc[gk[j]];
+			const float rv = b[(size_t)c * nh + k] - (a.lambda[c] * n.S * xk - (1.0f - a.lambda[c]) * lap);
+			s_r[(size_t)l * C + c] = rv;
+			s_dA[(size_t)l * C + c] = 0.f;
+			s_x[(size_t)l * C + c] = xk;
+			facc[c] = fmaf(rv, rv, facc[c]);
+		}
+	}
+	block_reduce(facc, partB);
+	cluster.sync();
+	double nr0[4], nr[4];
+	cluster_total(partB, nr0);
+	bool active[4];
+	int it[4];
+	float beta[4];
+#pragma unroll
+	for (int c = 0; c < 4; c++) {
+		nr[c] = (c < C) ? nr0[c] : 0.0;
+		active[c] = (c < C) && (nr0[c] > 0);
+		it[c] = 0;
+		beta[c] = 0.f;
+	}
+	int h = 0;  // direction buffer holding d_old: 0 -> dA, 1 -> dB
+	float q[kClusterPerThread][C];
+	for (;;) {
+		bool any = false;
+#pragma unroll
+		for (int c = 0; c < C; c++) any |= active[c];
+		if (!any) break;
+		float *dold = h ? s_dB : s_dA, *dnew = h ? s_dA : s_dB;
+		// d = r + beta d_old (own and neighbours) ; q = A d ; <r, q>
+#pragma unroll
+		for (int c = 0; c < 4; c++) facc[c] = 0.f;
+#pragma unroll
+		for (int u = 0; u < kClusterPerThread; u++) {
+			const int l = threadIdx.x + u * kClusterBlock;
+			if (l >= own) break;
+			const UnkC n = s_unk[l];
+			const uint32_t codes[4] = {n.ud >> 16, n.lr >> 16, n.ud & 0xFFFF, n.lr & 0xFFFF};
+			const float coefs[4] = {n.s_up, n.s_left, (n.links & 1) ? n.S : 0.f, (n.links & 2) ? n.S : 0.f};
+			const float sum = coefs[0] + coefs[1] + coefs[2] + coefs[3];
+			const float *nr_[4], *nd_[4];
+#pragma unroll
+			for (int j = 0; j < 4; j++) {
+				nr_[j] = (codes[j] != kNoNb) ? nb(0, codes[j]) : nullptr;
+				nd_[j] = (codes[j] != kNoNb) ? nb(1 + h, codes[j]) : nullptr;
+			}
+#pragma unroll
+			for (int c = 0; c < C; c++) {
+				if (!active[c]) continue;
+				const size_t o = (size_t)l * C + c;
+				const float rk = s_r[o];
+				const float dk = rk + beta[c] * dold[o];
+				float lap = -dk * sum;
+#pragma unroll
+				for (int j = 0; j < 4; j++)
+					if (codes[j] != kNoNb) lap += coefs[j] * (nr_[j][c] + beta[c] * nd_[j][c]);
+				const float qv = a.lambda[c] * n.S * dk - (1.0f - a.lambda[c]) * lap;
+				dnew[o] = dk;
+				q[u][c] = qv;
+				facc[c] = fmaf(rk, qv, facc[c]);
+			}
+		}
+		block_reduce(facc, partA);
+		cluster.sync();
+		double rq[4];
+		cluster_total(partA, rq);
+		if (threadIdx.x < C) s_coef[threadIdx.x] = active[threadIdx.x] ? (float)(nr[threadIdx.x] / rq[threadIdx.x]) : 0.f;
+		__syncthreads();
+		float alpha[4];
+#pragma unroll
+		for (int c = 0; c < C; c++) alpha[c] = s_coef[c];
+		// x += alpha d ; r -= alpha q ; |r|^2   (own unknowns only)
+#pragma unroll
+		for (int c = 0; c < 4; c++) facc[c] = 0.f;
+#pragma unroll
+		for (int u = 0; u < kClusterPerThread; u++) {
+			const int l = threadIdx.x + u * kClusterBlock;
+			if (l >= own) break;
+#pragma unroll
+			for (int c = 0; c < C; c++) {
+				if (!active[c]) continue;
+				const size_t o = (size_t)l * C + c;
+				s_x[o] += alpha[c] * dnew[o];
+				const float rv = s_r[o] - alpha[c] * q[u][c];
+				s_r[o] = rv;
+				facc[c] = fmaf(rv, rv, facc[c]);
+			}
+		}
+		// partA / partB are rewritten only after the next barrier, by which
+		// time every CTA has read them
+		block_reduce(facc, partB);
+		cluster.sync();
+		double nrn[4];
+		cluster_total(partB, nrn);
+		if (threadIdx.x < C) {
+			const int c = threadIdx.x;
+			if (active[c]) {
+				s_coef[c] = (float)(nrn[c] / nr[c]);
+				s_active[c] = ((nrn[c] < (double)a.tol * nr0[c]) || (it[c] >= a.limit)) ? 0 : 1;
+			}
+		}
+		__syncthreads();
+#pragma unroll
+		for (int c = 0; c < C; c++) {
+			if (!active[c]) continue;
+			beta[c] = s_coef[c];
+			nr[c] = nrn[c];
+			it[c]++;
+			active[c] = s_active[c] != 0;
+		}
+		__syncthreads();
+		h = 1 - h;
+	}
+	if (rank == 0 && threadIdx.x < C) iters_out[threadIdx.x] = it[threadIdx.x];
+	// u = orig + delta on the hole (:89-104)
+	double dacc = 0.0;
+	for (int l = threadIdx.x; l < own; l += blockDim.x) {
+		const int pix = hole[lo + l];
+#pragma unroll
+		for (int c = 0; c < C; c++) {
+			const float o = orig[(size_t)C * pix + c];
+			const float v = o + s_x[(size_t)l * C + c];
+			const float prev = img[(size_t)C * pix + c];
+			const float dd = prev - v;
+			dacc += (double)(dd * dd);
+			img[(size_t)C * pix + c] = v;
+		}
+	}
+	dacc = block_sum<kClusterBlock>(dacc, &red[0][0]);
+	if (threadIdx.x == 0) diff_part[rank] = dacc;
+	cluster.sync();  // no CTA leaves while others may still read its shared memory
+}
+
 __global__ void k_hole_index(const int32_t *__restrict__ hole, int nh, int32_t *__restrict__ index)
 {
 	const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -582,10 +861,73 @@ static void poisson_run(nli_ctx *ctx, const UpdArgs &u, const nli_update_params 
 	float *r = ctx->buf<float>("poi.r", (size_t)nh * C);
 	float *d = ctx->buf<float>("poi.d", (size_t)nh * C);
 	float *q = ctx->buf<float>("poi.q", (size_t)nh * C);
+	// shared-memory cluster kernel: kClusterVectors vectors x C channels x chunk floats per CTA
+	constexpr size_t kSmemBudget = 216 * 1024;
+	auto cluster_kernel = [](int CC) {
+		return (CC == 1) ? k_poisson_cg_cluster<1>
+		       : (CC == 2) ? k_poisson_cg_cluster<2> : (CC == 3) ? k_poisson_cg_cluster<3> : k_poisson_cg_cluster<4>;
+	};
+	if (ctx->cg_cluster_max < 0) {
+		// largest cluster the device runs with the biggest shared-memory footprint
+		int maxc = 0;
+		bool ok = true;
+		for (int CC = 1; CC <= 4; CC++) {
+			ok &= cudaFuncSetAttribute(cluster_kernel(CC), cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == 0;
+			ok &= cudaFuncSetAttribute(cluster_kernel(CC), cudaFuncAttributeMaxDynamicSharedMemorySize,
+			                           (int)kSmemBudget) == 0;
+		}
+		if (ok) {
+			cudaLaunchConfig_t qc = {};
+			qc.gridDim = dim3(kClusterMax);
+			qc.blockDim = dim3(kClusterBlock);
+			qc.dynamicSmemBytes = kSmemBudget;
+			if (cudaOccupancyMaxPotentialClusterSize(&maxc, cluster_kernel(4), &qc) != cudaSuccess) maxc = 0;
+		}
+		cudaGetLastError();
+		ctx->cg_cluster_max = std::min(maxc, kClusterMax);
+	}
+	int ncta = 0, chunk = 0;
+	if (ctx->cg_cluster_max >= 1) {
+		ncta = std::max(1, std::min(ctx->cg_cluster_max, (nh + 2 * kClusterBlock - 1) / (2 * kClusterBlock)));
+		chunk = (nh + ncta - 1) / ncta;
+		if ((size_t)kClusterVectors * C * chunk * sizeof(float) + chunk * sizeof(UnkC) > kSmemBudget ||
+		    chunk > kClusterMaxChunk)
+			ncta = chunk = 0;
+	}
 	{
 		ProfScope ps(ctx, "poisson_setup");
-		k_poisson_setup<<<(nh + 255) / 256, 256, 0, s>>>(pa, hole, hole_index, co, image, orig, unk, b, x);
+		k_poisson_setup<<<(nh + 255) / 256, 256, 0, s>>>(pa, chunk, hole, hole_index, co, image, orig, unk, b, x);
 		NLI_CHECK_LAUNCH();
+	}
+
+	int *iters = ctx->buf<int>("poi.iters", 4);
+	const float *orig_c = orig;
+	if (ncta > 0) {
+		const size_t smem = (size_t)kClusterVectors * C * chunk * sizeof(float) + chunk * sizeof(UnkC);
+		UnkC *unkc = ctx->buf<UnkC>("poi.unkc", nh);
+		k_poisson_compact<<<(nh + 255) / 256, 256, 0, s>>>(unk, nh, chunk, unkc);
+		NLI_CHECK_LAUNCH();
+		{
+			double *diff_part = ctx->buf<double>("poi.diff", ncta + 1);
+			cudaLaunchConfig_t cfg = {};
+			cfg.gridDim = dim3(ncta);
+			cfg.blockDim = dim3(kClusterBlock);
+			cfg.dynamicSmemBytes = smem;
+			cfg.stream = s;
+			cudaLaunchAttribute attr[1];
+			attr[0].id = cudaLaunchAttributeClusterDimension;
+			attr[0].val.clusterDim.x = ncta;
+			attr[0].val.clusterDim.y = 1;
+			attr[0].val.clusterDim.z = 1;
+			cfg.attrs = attr;
+			cfg.numAttrs = 1;
+			ProfScope ps(ctx, "poisson_cg");
+			NLI_CUDA(cudaLaunchKernelEx(&cfg, cluster_kernel(C), pa, chunk, (const UnkC *)unkc, (const float *)b,
+			                            (const float *)x, iters, hole, orig_c, image, diff_part));
+			nli_count_launch_internal();
+			*n_partials = ncta;
+			return;
+		}
 	}
 
 	int dev_blocks_per_sm = 0;
@@ -596,10 +938,8 @@ static void poisson_run(nli_ctx *ctx, const UpdArgs &u, const nli_update_params 
 	grid = std::min(std::max(grid, 1), std::min(max_blocks, ctx->num_sms));
 	double *part = ctx->buf<double>("poi.part", (size_t)grid * 8);
 	double *diff_part = ctx->buf<double>("poi.diff", grid + 1);
-	int *iters = ctx->buf<int>("poi.iters", 4);
 	NLI_CUDA(cudaMemsetAsync(ctx->status, 0, sizeof(DevStatus), s));
 	DevStatus *st = ctx->status;
-	const float *orig_c = orig;
 	void *args[] = {&pa, &unk, &b, &x, &r, &d, &q, &part, &st, &iters, (void *)&hole, &orig_c, &image, &diff_part};
 	{
 		ProfScope ps(ctx, "poisson_cg");
