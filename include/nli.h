@@ -233,6 +233,27 @@ int nli_distance_pairs(nli_ctx *ctx, const nli_distance_params *dist,
                        const float *target, int tW, int tH, int C,
                        const int32_t *pairs, int n, float *out);
 
+/* Allocation-free nli_distance_pairs, for callers that cannot allocate
+ * device memory while they run (a host framework that reserves the whole
+ * device budget up front, or a latency-critical loop in which cudaMalloc /
+ * cudaFree would synchronise the device).  No counterpart in the reference:
+ * it computes exactly what nli_distance_pairs computes, but takes no context,
+ * calls no cudaMalloc / cudaFree, and keeps its gradient images in a fixed
+ * device array of NLI_NOALLOC_SCRATCH_BYTES that every process loading this
+ * library holds on each device it uses until exit.  Work is enqueued on
+ * `stream` (a cudaStream_t, NULL = legacy default stream) of the current
+ * device.  The first call on a device looks up the array's device address;
+ * make that first call before any stream capture.  Returns NLI_E_INVALID
+ * when the gradients needed (sW*sH*2C floats, plus tW*tH*2C when target is
+ * a different image; none for the L2Norm/L1Norm kinds) exceed
+ * NLI_NOALLOC_SCRATCH_BYTES.  All calls share the array: calls that overlap
+ * on the GPU race and must be ordered by the caller. */
+#define NLI_NOALLOC_SCRATCH_BYTES (8u << 20)
+int nli_distance_pairs_noalloc(const nli_distance_params *dist,
+                               const float *source, int sW, int sH,
+                               const float *target, int tW, int tH, int C,
+                               const int32_t *pairs, int n, float *out, void *stream);
+
 /* Exhaustive nearest neighbour: for every target pixel with target_mask != 0,
  * the source pixel with source_mask != 0 of least distance (ties -> lowest
  * raster index y*sW + x).  Same arithmetic as nli_distance_pairs.  Points

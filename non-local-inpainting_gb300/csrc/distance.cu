@@ -1,6 +1,8 @@
 // APatchDistance::calculate over explicit pair lists, and the exhaustive
 // nearest-neighbour search used to pin PatchMatch on small crops.  Both use
 // the reference-exact distance (nli_device.cuh, dist_exact).
+#include <mutex>
+
 #include "nli_device.cuh"
 
 namespace nli {
@@ -135,6 +137,83 @@ extern "C" int nli_bruteforce_nnf(nli_ctx *ctx, const nli_distance_params *dist,
 		NLI_CHECK_LAUNCH();
 	} catch (const Error &e) {
 		ctx->last_error = e.message;
+		return e.status;
+	}
+	return NLI_OK;
+}
+
+// ------------------------------------------------------------------------
+// Allocation-free variant of nli_distance_pairs.
+//
+// Some callers cannot allocate device memory once they are running: host
+// frameworks that reserve the whole device budget up front and forbid any
+// further cudaMalloc, or latency-critical loops in which cudaMalloc /
+// cudaFree would synchronise the device.  This entry point needs no context
+// and no workspace: the gradient images it builds live in the fixed
+// file-scope array below, which every process that loads this library
+// holds on every device it uses until exit.  All calls share that array,
+// so calls that overlap on the GPU (different streams, or different host
+// threads without ordering) race on it; callers must order them.  Nothing
+// in the array needs to start at zero: every element a call reads is
+// written earlier in the same call.
+namespace nli {
+
+constexpr size_t kNoAllocScratchFloats = NLI_NOALLOC_SCRATCH_BYTES / sizeof(float);
+static __device__ __align__(256) float g_noalloc_scratch[kNoAllocScratchFloats];
+
+constexpr int kNoAllocMaxDevices = 64;
+static float *g_noalloc_ptr[kNoAllocMaxDevices];
+static std::mutex g_noalloc_mutex;
+
+// Device address of the scratch array on the current device, looked up
+// once per device (the first call on a device does this set-up).
+static float *noalloc_scratch(int device)
+{
+	std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+	if (!g_noalloc_ptr[device]) {
+		float *p = nullptr;
+		NLI_CUDA(cudaGetSymbolAddress((void **)&p, g_noalloc_scratch));
+		g_noalloc_ptr[device] = p;
+	}
+	return g_noalloc_ptr[device];
+}
+
+}  // namespace nli
+
+extern "C" int nli_distance_pairs_noalloc(const nli_distance_params *dist, const float *source, int sW, int sH,
+                                          const float *target, int tW, int tH, int C, const int32_t *pairs, int n,
+                                          float *out, void *stream)
+{
+	try {
+		if (!dist || !source || !target || !out || (!pairs && n > 0)) return NLI_E_INVALID;
+		if (sW <= 0 || sH <= 0 || tW <= 0 || tH <= 0 || n < 0) return NLI_E_INVALID;
+		DistArgs a;
+		fill_dist_args(a, *dist, C);
+		const bool grad = dist->kind == NLI_DIST_L2_COMBINED || dist->kind == NLI_DIST_L2_RGBD;
+		const bool same = target == source && tW == sW && tH == sH;
+		const size_t gs = grad ? (size_t)sW * sH * 2 * C : 0;
+		const size_t gt = (grad && !same) ? (size_t)tW * tH * 2 * C : 0;
+		if (gs + gt > kNoAllocScratchFloats) return NLI_E_INVALID;  // beyond NLI_NOALLOC_SCRATCH_BYTES
+		if (n == 0) return NLI_OK;
+		int device = 0;
+		NLI_CUDA(cudaGetDevice(&device));
+		if (device < 0 || device >= kNoAllocMaxDevices) return NLI_E_UNSUPPORTED;
+		float *scratch = noalloc_scratch(device);
+		cudaStream_t s = (cudaStream_t)stream;
+		const float *grad_s = nullptr, *grad_t = nullptr;
+		if (grad) {
+			launch_gradient(s, source, sW, sH, C, scratch);
+			grad_s = scratch;
+			grad_t = scratch;
+			if (!same) {
+				launch_gradient(s, target, tW, tH, C, scratch + gs);
+				grad_t = scratch + gs;
+			}
+		}
+		k_distance_pairs<<<(n + 127) / 128, 128, 0, s>>>(a, source, grad_s, sW, sH, target, grad_t, tW, tH,
+		                                                  reinterpret_cast<const int4 *>(pairs), n, out);
+		NLI_CHECK_LAUNCH();
+	} catch (const Error &e) {
 		return e.status;
 	}
 	return NLI_OK;
