@@ -1,0 +1,3 @@
+/* Forwarding header with the reference's name (l2_combined_patch_distance.h): the drop-in classes
+ * are declared in nli_inpainting.hpp. */
+#include "../nli_inpainting.hpp"

@@ -11,6 +11,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnli_gb300.so")
+DROPIN = os.path.join(HERE, "libnli_dropin.so")
+CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
 SOURCES = ["api.cu", "gradient.cu", "distance.cu", "patchmatch.cu", "update.cu", "pyramid.cu", "process.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -62,7 +64,21 @@ def build(force=False, verbose=False, extra=()):
     if force or jobs or _stale(LIB, objs):
         _run([nvcc, *ARCH, "-shared", *objs, "-o", LIB + ".tmp", "-lcudart"])
         os.replace(LIB + ".tmp", LIB)
+    build_dropin(force)
     return LIB
+
+
+def build_dropin(force=False):
+    """libnli_dropin.so: the C++ classes of include/nli_inpainting.hpp over the C ABI."""
+    src = os.path.join(CSRC, "dropin.cpp")
+    deps = [src, LIB, os.path.join(ROOT, "include", "nli_inpainting.hpp"), os.path.join(ROOT, "include", "nli.h")]
+    if not force and not _stale(DROPIN, deps):
+        return DROPIN
+    _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-I", os.path.join(ROOT, "include"),
+          "-I", os.path.join(CUDA_HOME, "include"), src, "-o", DROPIN + ".tmp", "-L", HERE, "-lnli_gb300",
+          "-L", os.path.join(CUDA_HOME, "lib64"), "-lcudart", "-Wl,-rpath,$ORIGIN"])
+    os.replace(DROPIN + ".tmp", DROPIN)
+    return DROPIN
 
 
 if __name__ == "__main__":
