@@ -207,7 +207,6 @@ def run_ours(args):
     pkg = ge.package()
     ge.build() if not os.path.exists(pkg.LIB_PATH) else None
     ctx = pkg.Context(local)
-    ctx.set_seed(1234 + rank)
     img, mask, p = workload()
     H, W, C = img.shape
     mpix = W * H / 1e6
@@ -235,7 +234,11 @@ def run_ours(args):
             ms.append(a.elapsed_time(b))
         return ms
 
+    seed = 1234 + rank
+
     def step():
+        # the same seed every step: every step does the same work
+        ctx.set_seed(seed)
         ctx.process_device(d_img, d_mask, p, out=d_out)
 
     for _ in range(args.warmup):
@@ -267,6 +270,7 @@ def run_ours(args):
     st = pkg.ProcessStats()
 
     def e2e_step():
+        ctx.set_seed(seed)
         rc = ctx.lib.nli_process(ctx.h, ct.byref(p), ct.c_void_p(h_img.data_ptr()), ct.c_void_p(h_mask.data_ptr()),
                                  W, H, C, ct.c_void_p(h_out.data_ptr()), ct.byref(st))
         if rc != 0:

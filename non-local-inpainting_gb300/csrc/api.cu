@@ -67,7 +67,6 @@ void fill_dist_args(DistArgs &a, const nli_distance_params &p, int C)
 	a.rx = p.patch_x / 2;
 	a.ry = p.patch_y / 2;
 	a.C = C;
-	feature_layout(p.kind, C, &a.p4, &a.f1);
 	a.lambda = p.lambda;
 	a.lambda_d = p.lambda_d;
 	std::vector<float> w = gaussian_weights_host(p.patch_x, p.patch_y, p.sigma, p.sigma);

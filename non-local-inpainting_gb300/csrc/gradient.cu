@@ -1,5 +1,5 @@
-// Gradient::calculate (gradient.cpp:20-75), the packed feature image read
-// by the PatchMatch distance, mask compaction and small reductions.
+// Gradient::calculate (gradient.cpp:20-75), the padded pixel image read by
+// the PatchMatch distance, mask compaction and small reductions.
 #include "nli_device.cuh"
 
 namespace nli {
@@ -28,54 +28,28 @@ void launch_gradient(cudaStream_t s, const float *img, int W, int H, int C, floa
 	NLI_CHECK_LAUNCH();
 }
 
-// Features read by the PatchMatch distance, plane-major: per pixel the
-// components [u_0..u_{C-1}, gx_0, gy_0, ..., gx_{C-1}, gy_{C-1}] (gradient
-// kinds) or [u_0..u_{C-1}] (colour-only kinds); components 4j..4j+3 go to
-// float4 plane j (p4 planes of W*H float4), a ninth component (C = 3
-// gradient kinds: 9 components, 36 bytes per pixel) to one float plane.
-// Missing components of the last float4 are zero.
-void feature_layout(int kind, int C, int *p4, int *f1)
+// Pixels read by the PatchMatch distance: one float4 per pixel (channels
+// 0..C-1, the rest zero) over (W + 1) x (H + 1), the extra column and row
+// repeating the last ones so that forward differences there are exactly 0.
+__global__ void k_pad4(const float *__restrict__ img, int W, int H, int C, float4 *__restrict__ out)
 {
-	const int comps = (kind == NLI_DIST_L2_COMBINED || kind == NLI_DIST_L2_RGBD) ? 3 * C : C;
-	*f1 = (comps % 4 == 1 && comps > 1) ? 1 : 0;
-	*p4 = (comps - *f1 + 3) / 4;
-}
-
-template <bool GRAD>
-__global__ void k_features(const float *__restrict__ img, int W, int H, int C, int p4, int f1,
-                           float4 *__restrict__ planes4, float *__restrict__ plane1)
-{
-	const int n = W * H;
-	for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-		const int x = p % W, y = p / W;
-		float f[16];
-#pragma unroll
-		for (int k = 0; k < 16; k++) f[k] = 0.f;
-		const float *u = img + (size_t)p * C;
-		for (int c = 0; c < C; c++) {
-			const float v = u[c];
-			f[c] = v;
-			if (GRAD) {
-				f[C + 2 * c] = (x == W - 1) ? 0.0f : __fsub_rn(u[C + c], v);
-				f[C + 2 * c + 1] = (y == H - 1) ? 0.0f : __fsub_rn(u[(size_t)C * W + c], v);
-			}
-		}
-		for (int k = 0; k < p4; k++)
-			planes4[(size_t)k * n + p] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);
-		if (f1) plane1[p] = f[4 * p4];
+	const int Wp = W + 1, n = Wp * (H + 1);
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		const int y = i / Wp, x = i - y * Wp;
+		const float *u = img + ((size_t)min(y, H - 1) * W + min(x, W - 1)) * C;
+		float4 v = make_float4(u[0], 0.f, 0.f, 0.f);
+		if (C > 1) v.y = u[1];
+		if (C > 2) v.z = u[2];
+		if (C > 3) v.w = u[3];
+		out[i] = v;
 	}
 }
 
-void launch_features(cudaStream_t s, int kind, const float *img, int W, int H, int C, float4 *planes4, float *plane1)
+void launch_pad4(cudaStream_t s, const float *img, int W, int H, int C, float4 *out)
 {
-	const int n = W * H;
+	const int n = (W + 1) * (H + 1);
 	const int block = 256, grid = (n + block - 1) / block;
-	int p4, f1;
-	feature_layout(kind, C, &p4, &f1);
-	if (kind == NLI_DIST_L2_COMBINED || kind == NLI_DIST_L2_RGBD)
-		k_features<true><<<grid, block, 0, s>>>(img, W, H, C, p4, f1, planes4, plane1);
-	else
-		k_features<false><<<grid, block, 0, s>>>(img, W, H, C, p4, f1, planes4, plane1);
+	k_pad4<<<grid, block, 0, s>>>(img, W, H, C, out);
 	NLI_CHECK_LAUNCH();
 }
 

@@ -37,18 +37,22 @@ __device__ __forceinline__ uint4 philox(uint4 c, uint2 k)
 	return c;
 }
 
-// A stream of 32-bit draws for one (pixel, sweep) pair: four draws per
-// Philox block, counter = (pixel, sweep, block index, 0).
+// A stream of 32-bit draws for one (pixel, sweep, stream) triple: four
+// draws per Philox block, counter = (pixel, sweep, block index, tag ^
+// stream << 16).
 struct Rng {
 	uint2 key;
-	uint32_t pixel, sweep, block;
+	uint32_t pixel, sweep, block, tag;
 	uint4 cur;
 	int used;
-	__device__ Rng(uint2 k, uint32_t p, uint32_t s) : key(k), pixel(p), sweep(s), block(0), used(4) {}
+	__device__ Rng(uint2 k, uint32_t p, uint32_t s, uint32_t stream = 0)
+	    : key(k), pixel(p), sweep(s), block(0), tag(0x6e6c6900u ^ (stream << 16)), used(4)
+	{
+	}
 	__device__ __forceinline__ uint32_t next()
 	{
 		if (used == 4) {
-			cur = philox(make_uint4(pixel, sweep, block++, 0x6e6c6900u), key);
+			cur = philox(make_uint4(pixel, sweep, block++, tag), key);
 			used = 0;
 		}
 		uint32_t r = (used == 0) ? cur.x : (used == 1) ? cur.y : (used == 2) ? cur.z : cur.w;

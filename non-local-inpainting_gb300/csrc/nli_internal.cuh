@@ -177,7 +177,6 @@ struct DistArgs {
 	int kind;
 	int px, py, rx, ry;  // patch size and radius (radius = size / 2)
 	int C;               // image channels
-	int p4, f1;          // feature planes: float4 planes and float planes (see feature_layout)
 	float lambda, lambda_d;
 	float weights[kMaxTaps];  // Gaussian patch weights, row-major
 };
@@ -185,13 +184,12 @@ struct DistArgs {
 // ---------------------------------------------------------- host helpers
 std::vector<float> gaussian_weights_host(unsigned sx, unsigned sy, float sigma_x, float sigma_y);
 void fill_dist_args(DistArgs &a, const nli_distance_params &p, int C);
-void feature_layout(int kind, int C, int *p4, int *f1);
 
 // ------------------------------------------------------------- launchers
 // gradient.cu
 void launch_gradient(cudaStream_t s, const float *img, int W, int H, int C, float *grad);
-// Plane-major feature image of the PatchMatch distance (gradient.cu).
-void launch_features(cudaStream_t s, int kind, const float *img, int W, int H, int C, float4 *planes4, float *plane1);
+// Padded float4 pixel image read by the PatchMatch distance (gradient.cu).
+void launch_pad4(cudaStream_t s, const float *img, int W, int H, int C, float4 *out);
 
 // compact.cu: raster-order list of the pixels with mask != 0; returns count
 int compact_mask(nli_ctx *ctx, const uint8_t *mask, int W, int H, int32_t *list, const char *tag);

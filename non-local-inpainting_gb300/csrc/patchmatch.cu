@@ -11,32 +11,55 @@
 //   2. random search around the best match after propagation, in windows
 //      max(W,H), /2, ..., 1 with up to `random_shots` draws per window and
 //      the first draw that lands in the source evaluated (:458-494).
-// A candidate equal to the current match is not re-evaluated.  Random draws
-// come from Philox4x32-10 keyed by the context seed and call counter.
+// A candidate equal to the current match, or to an earlier candidate of the
+// same step, is not re-evaluated (its distance would not be smaller).
+// Random draws come from Philox4x32-10 keyed by the context seed and call
+// counter.
 //
-// One warp works on one target point at a time (persistent warps).  Lane l
-// holds taps l, l + 32, ... of the target patch in registers and reads the
-// same taps of every candidate source patch from the plane-major feature
-// image (36 bytes per pixel for 3 channels); the weighted distance is
-// summed with a butterfly of shuffles.  All control flow is warp-uniform.
+// Layout and work split.  Images are read as one float4 per pixel (the C
+// channels, zero-filled), with one extra column and row that repeat the
+// last ones, so the forward differences u(x+1) - u(x) and u(y+1) - u(y) are
+// exactly 0 on the last column / row, as Gradient::calculate sets them
+// (gradient.cpp:37-63).  One warp works on one target point at a time
+// (persistent warps); its target window (patch + 1 column + 1 row) sits in
+// shared memory.  The warp's lanes are split into K = 32 / L sub-warps of
+// L = patch width + 1 lanes (3 sub-warps of 10 lanes for 9x9 patches); each
+// sub-warp evaluates one candidate, lane c walking down column c of the
+// candidate's window.  Per row a lane loads one float4, forms the colour
+// difference d = u_s - u_t, gets d of column c + 1 by a shuffle (x gradient
+// difference) and keeps the previous row's d in registers (y gradient
+// difference).  The gradient difference of the two patches is formed as a
+// difference of colour differences, (u_s(x+1) - u_t(x+1)) - (u_s(x) - u_t(x)),
+// which equals (gx_s - gx_t) up to float rounding.  The candidates of one
+// step (propagation, then random search) are gathered first, one per lane,
+// then evaluated K at a time and accepted in their sequential order with a
+// strict "<", so the result equals evaluating them one after the other.
 #include "nli_device.cuh"
 
 namespace nli {
 
+constexpr unsigned kFull = 0xffffffffu;
+
 struct PmArgs {
-	const float4 *fs4;  // source feature planes (P4 float4 planes of sW*sH)
-	const float *fs1;   // source float plane (F1 == 1)
-	const float4 *ft4;  // target feature planes
-	const float *ft1;
+	const float4 *src;  // source pixels, (sW + 1) x (sH + 1), row stride sWp
+	const float4 *tgt;  // target pixels, row stride tWp
 	const uint8_t *smask;
 	const uint8_t *tmask;
 	const int32_t *tlist;
 	int sW, sH, tW, tH, nt;
-	int sN, tN;  // pixels per plane
+	int sWp, tWp;
 	int shots, max_window;
 	uint2 key;
 	// patch extent around a centre: [x - rx, x + ex) x [y - ry, y + ey)
 	int rx, ry, ex, ey;
+	// lanes per candidate, candidates per warp step, window rows
+	int L, K, rows;
+	float lambda, lambda_d;
+};
+
+template <int KIND>
+struct Kind {
+	static constexpr bool grad = KIND == NLI_DIST_L2_COMBINED || KIND == NLI_DIST_L2_RGBD;
 };
 
 // A source centre is usable when it is in the source mask and its whole
@@ -57,199 +80,304 @@ __device__ __forceinline__ bool tgt_ok(const PmArgs &p, int x, int y)
 	return (unsigned)x < (unsigned)p.tW && (unsigned)y < (unsigned)p.tH && p.tmask[y * p.tW + x];
 }
 
-// Feature planes of a (distance kind, channel count): P4 float4 planes and
-// F1 float planes (same rule as feature_layout).
-template <int KIND, int C>
-struct Layout {
-	static constexpr int comps = (KIND == NLI_DIST_L2_COMBINED || KIND == NLI_DIST_L2_RGBD) ? 3 * C : C;
-	static constexpr int F1 = (comps % 4 == 1 && comps > 1) ? 1 : 0;
-	static constexpr int P4 = (comps - F1 + 3) / 4;
-	static constexpr int N = 4 * P4 + F1;
-};
+// Shared memory: per-tap weights (divided by the patch area) for all warps,
+// padded to a float4 boundary, then one target window of rows x L float4
+// per warp, then one 32-entry candidate list per warp.
+__host__ __device__ inline int pm_weight_slots(int taps) { return (taps + 3) / 4; }
 
-// Per-lane tap table: lane l owns taps l, l + 32, ... (NT slots); offsets
-// and weights (already multiplied by the term coefficients and by
-// 1 / patch area) are computed once per warp.
-template <int NT>
-struct TapTable {
-	int soff[NT], toff[NT];
-	float wa[NT], wb[NT], wc[NT], wd[NT];
-	bool valid[NT];
-};
-
-template <int KIND, int NT>
-__device__ __forceinline__ void make_taps(const DistArgs &a, const PmArgs &p, TapTable<NT> &T)
+__host__ __device__ inline size_t pm_smem_bytes(int taps, int rows, int L, int warps)
 {
-	const int lane = threadIdx.x & 31;
+	return sizeof(float4) * ((size_t)pm_weight_slots(taps) + (size_t)warps * rows * L) + sizeof(int) * 32 * warps;
+}
+
+__device__ __forceinline__ void load_weights(const DistArgs &a, float *s_w)
+{
 	const int taps = a.px * a.py;
 	const float invP = 1.0f / (float)taps;
-#pragma unroll
-	for (int k = 0; k < NT; k++) {
-		const int t = lane + 32 * k;
-		T.valid[k] = t < taps;
-		const int dy = t / a.px, dx = t - dy * a.px;
-		T.soff[k] = (dy - a.ry) * p.sW + (dx - a.rx);
-		T.toff[k] = (dy - a.ry) * p.tW + (dx - a.rx);
-		const float w = T.valid[k] ? a.weights[t] * invP : 0.f;
-		if (KIND == NLI_DIST_L2_NORM || KIND == NLI_DIST_L1_NORM) {
-			T.wa[k] = w;
-			T.wb[k] = T.wc[k] = T.wd[k] = 0.f;
-		} else {
-			T.wa[k] = w * a.lambda;
-			T.wb[k] = w * (1.0f - a.lambda);
-			T.wc[k] = w * a.lambda_d;
-			T.wd[k] = w * (1.0f - a.lambda_d);
-		}
-	}
+	for (int t = threadIdx.x; t < taps; t += blockDim.x) s_w[t] = a.weights[t] * invP;
+	__syncthreads();
 }
 
-// Feature components of tap slot k of pixel `pix` (+ the slot's offset).
-template <int KIND, int C, int NT>
-__device__ __forceinline__ void load_comps(const float4 *__restrict__ f4, const float *__restrict__ f1, int npix,
-                                           int pix, float (&f)[Layout<KIND, C>::N])
+// The warp's target window: rows x L pixels starting at the patch corner.
+// With up to 3 channels the unused fourth component carries the tap's
+// weight (0 outside the patch), so the distance reads one float4 per row.
+template <int C>
+__device__ __forceinline__ void load_window(const PmArgs &p, const float *s_w, int x, int y, float4 *s_t)
 {
-	using L = Layout<KIND, C>;
-#pragma unroll
-	for (int j = 0; j < L::P4; j++) {
-		const float4 v = __ldg(f4 + (size_t)j * npix + pix);
-		f[4 * j + 0] = v.x;
-		f[4 * j + 1] = v.y;
-		f[4 * j + 2] = v.z;
-		f[4 * j + 3] = v.w;
+	const int lane = threadIdx.x & 31;
+	const int px = p.rx + p.ex, py = p.ry + p.ey;
+	const float4 *T = p.tgt + (size_t)(y - p.ry) * p.tWp + (x - p.rx);
+	for (int e = lane; e < p.rows * p.L; e += 32) {
+		const int r = e / p.L, c = e - r * p.L;
+		float4 v = __ldg(T + (size_t)r * p.tWp + c);
+		if (C <= 3) v.w = (r < py && c < px) ? s_w[r * px + c] : 0.f;
+		s_t[e] = v;
 	}
-	if (L::F1) f[4 * L::P4] = __ldg(f1 + pix);
+	__syncwarp();
 }
 
-// The warp's target patch in shared memory: lane l keeps its slot k as
-// float4 planes at v4[(k * P4 + j) * 32 + l] and the float plane at
-// v1[k * 32 + l].  Each lane writes and reads only its own slots, so no
-// synchronisation is needed.
-template <int KIND, int C, int NT>
-struct TargetPatch {
-	float4 *v4;
-	float *v1;
+template <int C>
+__device__ __forceinline__ float sq3(float4 d)
+{
+	float n = d.x * d.x;
+	if (C > 1) n = fmaf(d.y, d.y, n);
+	if (C > 2) n = fmaf(d.z, d.z, n);
+	return n;
+}
+
+// sum of squares / absolute values over the first C components
+template <int C>
+__device__ __forceinline__ float sqc(float4 d)
+{
+	float n = sq3<C>(d);
+	if (C > 3) n = fmaf(d.w, d.w, n);
+	return n;
+}
+
+template <int C>
+__device__ __forceinline__ float absc(float4 d)
+{
+	float n = fabsf(d.x);
+	if (C > 1) n += fabsf(d.y);
+	if (C > 2) n += fabsf(d.z);
+	if (C > 3) n += fabsf(d.w);
+	return n;
+}
+
+// a - b over the first C components (the others are left 0)
+template <int C>
+__device__ __forceinline__ float4 subc(float4 a, float4 b)
+{
+	return make_float4(a.x - b.x, (C > 1) ? a.y - b.y : 0.f, (C > 2) ? a.z - b.z : 0.f, (C > 3) ? a.w - b.w : 0.f);
+}
+
+template <int C>
+__device__ __forceinline__ float4 shfl_down4(float4 v, int o)
+{
+	float4 r;
+	r.x = __shfl_down_sync(kFull, v.x, o);
+	r.y = (C > 1) ? __shfl_down_sync(kFull, v.y, o) : 0.f;
+	r.z = (C > 2) ? __shfl_down_sync(kFull, v.z, o) : 0.f;
+	r.w = (C > 3) ? __shfl_down_sync(kFull, v.w, o) : 0.f;
+	return r;
+}
+
+// Sum over the L lanes of each sub-warp, left in its lane c == 0.
+__device__ __forceinline__ float subwarp_sum(float v, int c, int L)
+{
+#pragma unroll
+	for (int o = 1; o < 16; o <<= 1) {
+		const float u = __shfl_down_sync(kFull, v, o);
+		if (c + o < L) v += u;
+	}
+	return v;
+}
+
+// Per-lane sums of one candidate by term: colour and gradient differences
+// of the colour channels (n, g) and of the depth channel (nd, gd, L2 RGBD).
+struct Acc {
+	float n, g, nd, gd;
 };
 
-template <int KIND, int C, int NT>
-__device__ __forceinline__ TargetPatch<KIND, C, NT> warp_target_slot()
+// Contribution of one window row.  d: colour difference of this lane's
+// pixel in row r, dp: of the row above; w, wp: their tap weights.
+template <int KIND, int C>
+__device__ __forceinline__ void row_terms(const float4 d, const float4 dp, float w, float wp, bool tap, bool tap_above,
+                                          Acc &A)
 {
-	using L = Layout<KIND, C>;
-	extern __shared__ float4 s_target[];
-	constexpr int per_warp4 = NT * L::P4 * 32 + (NT * L::F1 * 32 + 3) / 4;
-	TargetPatch<KIND, C, NT> P;
-	P.v4 = s_target + (size_t)(threadIdx.x >> 5) * per_warp4;
-	P.v1 = reinterpret_cast<float *>(P.v4 + NT * L::P4 * 32);
-	return P;
-}
-
-template <int KIND, int C, int NT>
-constexpr size_t target_smem_bytes(int warps)
-{
-	using L = Layout<KIND, C>;
-	return (size_t)warps * (NT * L::P4 * 32 + (NT * L::F1 * 32 + 3) / 4) * sizeof(float4);
-}
-
-template <int KIND, int C, int NT>
-__device__ __forceinline__ void load_target(const TapTable<NT> &T, const PmArgs &p, int tpix, TargetPatch<KIND, C, NT> &P)
-{
-	using L = Layout<KIND, C>;
-	const int lane = threadIdx.x & 31;
-#pragma unroll
-	for (int k = 0; k < NT; k++) {
-		const int q = tpix + T.toff[k];
-#pragma unroll
-		for (int j = 0; j < L::P4; j++)
-			P.v4[(k * L::P4 + j) * 32 + lane] =
-			    T.valid[k] ? __ldg(p.ft4 + (size_t)j * p.tN + q) : make_float4(0.f, 0.f, 0.f, 0.f);
-		if (L::F1) P.v1[k * 32 + lane] = T.valid[k] ? __ldg(p.ft1 + q) : 0.f;
+	if (KIND == NLI_DIST_L1_NORM) {
+		if (tap) A.n = fmaf(w, absc<C>(d), A.n);
+		return;
+	}
+	if (KIND == NLI_DIST_L2_NORM) {
+		if (tap) A.n = fmaf(w, sqc<C>(d), A.n);
+		return;
+	}
+	// x gradient difference from the lane to the right (column c + 1)
+	const float4 dr = shfl_down4<C>(d, 1);
+	if (KIND == NLI_DIST_L2_RGBD) {
+		if (tap) {
+			const float4 gx = subc<4>(dr, d);
+			A.n = fmaf(w, sq3<3>(d), A.n);
+			A.g = fmaf(w, sq3<3>(gx), A.g);
+			A.nd = fmaf(w, d.w * d.w, A.nd);
+			A.gd = fmaf(w, gx.w * gx.w, A.gd);
+		}
+		if (tap_above) {
+			const float4 gy = subc<4>(d, dp);
+			A.g = fmaf(wp, sq3<3>(gy), A.g);
+			A.gd = fmaf(wp, gy.w * gy.w, A.gd);
+		}
+	} else {
+		if (tap) {
+			const float4 gx = subc<C>(dr, d);
+			A.n = fmaf(w, sqc<C>(d), A.n);
+			A.g = fmaf(w, sqc<C>(gx), A.g);
+		}
+		if (tap_above) {
+			const float4 gy = subc<C>(d, dp);
+			A.g = fmaf(wp, sqc<C>(gy), A.g);
+		}
 	}
 }
 
-// Distance of the target patch to the source patch centred at pixel spix;
-// every lane returns the full sum.  All terms are non-negative, so once the
-// sum over the first 32 taps reaches `bound` the candidate cannot beat the
-// current match: that partial sum (>= bound) is returned without reading
-// the rest of the patch (exact early termination).
-template <int KIND, int C, int NT>
-__device__ __forceinline__ float warp_distance(const TapTable<NT> &T, const TargetPatch<KIND, C, NT> &P,
-                                               const PmArgs &p, int spix, float bound, unsigned &partial)
+// The lane's share of the distance: the terms weighted by lambda, 1 - lambda
+// (and lambda_d, 1 - lambda_d for the depth channel).
+template <int KIND>
+__device__ __forceinline__ float combine(const Acc &A, const PmArgs &p)
 {
-	float r = 0.f, head = 0.f;
-#pragma unroll
-	for (int k = 0; k < NT; k++) {
-		if (k == 1) {
-#pragma unroll
-			for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
-			head = r;
-			if (head >= bound) {
-				partial++;
-				return head;
+	if (KIND == NLI_DIST_L1_NORM || KIND == NLI_DIST_L2_NORM) return A.n;
+	float v = fmaf(p.lambda, A.n, (1.0f - p.lambda) * A.g);
+	if (KIND == NLI_DIST_L2_RGBD) v = fmaf(p.lambda_d, A.nd, fmaf(1.0f - p.lambda_d, A.gd, v));
+	return v;
+}
+
+// Evaluates the n candidates held one per lane (packed x | y << 16, lane i
+// holds candidate i) against the target window s_t, in steps of K, and
+// accepts each in order when strictly better than the current match.  All
+// lanes return the same best / bd.  Once the rows summed so far reach the
+// current distance for every candidate of a step, the rest of the step is
+// skipped (exact: all terms are non-negative).  P > 0: square P x P patch
+// known at compile time (rows unrolled); P == 0: sizes from the arguments.
+template <int KIND, int C, int P>
+__device__ __forceinline__ void eval_candidates(const PmArgs &p, const float *s_w, const float4 *s_t, int mycand,
+                                                int n, int2 &best, float &bd, unsigned &partial)
+{
+	constexpr bool G = Kind<KIND>::grad;
+	constexpr int PF = (C == 4) ? 1 : 2;  // rows of loads in flight (fewer for 4 channels: registers)
+	const int L = P ? P + G : p.L;
+	const int K = P ? 32 / (P + G) : p.K;
+	const int rows = P ? P + G : p.rows;
+	const int px = P ? P : p.rx + p.ex;
+	const int py = P ? P : p.ry + p.ey;
+	const int lane = threadIdx.x & 31;
+	const int sw = lane / L, c = lane - sw * L;
+	const bool tapcol = c < px;
+	const int check_row = rows / 2;
+	const size_t sWp = (size_t)p.sWp;
+	const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 1
+	for (int b = 0; b < n; b += K) {
+		const int idx = b + sw;
+		const bool active = sw < K && idx < n;
+		const bool act_col = active && tapcol;
+		const int cand = __shfl_sync(kFull, mycand, active ? idx : 0);
+		const int cx = cand & 0xffff, cy = cand >> 16;
+		const float4 *S = p.src + (size_t)(cy - p.ry) * sWp + (cx - p.rx) + c;
+		const float4 *T = s_t + c;
+		const float *Wt = s_w + c;
+		float4 v0 = active ? __ldg(S) : zero;
+		float4 v1 = (PF == 2 && active && rows > 1) ? __ldg(S + sWp) : zero;
+		float4 dp = zero;
+		float wp = 0.f;
+		Acc A = {0.f, 0.f, 0.f, 0.f};
+		const float bound = bd;
+		bool stop = false;
+		auto row = [&](int r) {
+			const float4 v = v0;
+			if (PF == 2) {
+				v0 = v1;
+				v1 = (active && r + 2 < rows) ? __ldg(S + (size_t)(r + 2) * sWp) : zero;
+			} else {
+				v0 = (active && r + 1 < rows) ? __ldg(S + (size_t)(r + 1) * sWp) : zero;
 			}
-			r = 0.f;
-		}
-		if (!T.valid[k]) continue;
-		using L = Layout<KIND, C>;
-		const int lane = threadIdx.x & 31;
-		float f[L::N];
-		load_comps<KIND, C, NT>(p.fs4, p.fs1, p.sN, spix + T.soff[k], f);
+			const float4 t = T[r * L];
+			const float4 d = subc<C>(v, t);
+			const bool tap = act_col && r < py;
+			const float w = (C <= 3) ? t.w : (tap ? Wt[r * px] : 0.f);
+			row_terms<KIND, C>(d, dp, w, wp, tap, G && act_col && r > 0, A);
+			dp = d;
+			wp = w;
+		};
+		auto check = [&]() {
+			const float part = subwarp_sum(combine<KIND>(A, p), c, L);
+			return __all_sync(kFull, !active || c != 0 || part >= bound);
+		};
+		if constexpr (P > 0) {
 #pragma unroll
-		for (int j = 0; j < L::P4; j++) {
-			const float4 t4 = P.v4[(k * L::P4 + j) * 32 + lane];
-			f[4 * j + 0] -= t4.x;
-			f[4 * j + 1] -= t4.y;
-			f[4 * j + 2] -= t4.z;
-			f[4 * j + 3] -= t4.w;
-		}
-		if (L::F1) f[4 * L::P4] -= P.v1[k * 32 + lane];
-		if (KIND == NLI_DIST_L1_NORM) {
-			float n = 0.f;
-#pragma unroll
-			for (int c = 0; c < C; c++) n += fabsf(f[c]);
-			r = fmaf(T.wa[k], n, r);
-		} else if (KIND == NLI_DIST_L2_NORM) {
-			float n = 0.f;
-#pragma unroll
-			for (int c = 0; c < C; c++) n = fmaf(f[c], f[c], n);
-			r = fmaf(T.wa[k], n, r);
-		} else if (KIND == NLI_DIST_L2_RGBD) {
-			float n = 0.f, g = 0.f;
-#pragma unroll
-			for (int c = 0; c < 3; c++) n = fmaf(f[c], f[c], n);
-#pragma unroll
-			for (int c = 0; c < 6; c++) g = fmaf(f[4 + c], f[4 + c], g);
-			r = fmaf(T.wa[k], n, r);
-			r = fmaf(T.wb[k], g, r);
-			r = fmaf(T.wc[k], f[3] * f[3], r);
-			r = fmaf(T.wd[k], fmaf(f[10], f[10], f[11] * f[11]), r);
+			for (int r = 0; r < P + G; r++) {
+				row(r);
+				if (r == (P + G) / 2 && check()) {
+					stop = true;
+					break;
+				}
+			}
 		} else {
-			float n = 0.f, g = 0.f;
-#pragma unroll
-			for (int c = 0; c < C; c++) n = fmaf(f[c], f[c], n);
-#pragma unroll
-			for (int c = 0; c < 2 * C; c++) g = fmaf(f[C + c], f[C + c], g);
-			r = fmaf(T.wa[k], n, r);
-			r = fmaf(T.wb[k], g, r);
+#pragma unroll 1
+			for (int r = 0; r < rows; r++) {
+				row(r);
+				if (r == check_row && check()) {
+					stop = true;
+					break;
+				}
+			}
+		}
+		const int in_step = min(K, n - b);
+		if (stop) {
+			partial += in_step;
+			continue;
+		}
+		const float sum = subwarp_sum(combine<KIND>(A, p), c, L);
+#pragma unroll 1
+		for (int s = 0; s < in_step; s++) {
+			const float ds = __shfl_sync(kFull, sum, s * L);
+			if (ds < bd) {
+				bd = ds;
+				const int q = __shfl_sync(kFull, mycand, b + s);
+				best = make_int2(q & 0xffff, q >> 16);
+			}
 		}
 	}
-#pragma unroll
-	for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
-	return head + r;
 }
 
-// threads per block: one 32-warp block per SM for patches up to 96 taps;
-// 8-warp blocks for larger patches (their target patches need more shared
-// memory per warp)
-template <int NT>
-constexpr int pm_block() { return NT > 3 ? 256 : 1024; }
-
-template <int KIND, int C, int NT>
-__global__ void __launch_bounds__(pm_block<NT>(), NT > 3 ? 2 : 1) k_pm_init(DistArgs a, PmArgs p, const int2 *__restrict__ init,
-                                                    int2 *__restrict__ nnf, float *__restrict__ dist,
-                                                    unsigned long long *counter)
+// Candidates proposed one per lane, in lane order: keeps the valid ones that
+// differ from the current match and from every lower lane's candidate and
+// moves them to lanes 0..n-1 (mycand), in order.  Returns n.
+__device__ __forceinline__ int compact_candidates(bool valid, int packed, const int2 &best, int *s_list, int &mycand)
 {
 	const int lane = threadIdx.x & 31;
-	TapTable<NT> T;
-	make_taps<KIND, NT>(a, p, T);
+	const unsigned below = (1u << lane) - 1u;
+	valid = valid && packed != (best.x | (best.y << 16));
+	const unsigned vmask = __ballot_sync(kFull, valid);
+	const unsigned same = __match_any_sync(kFull, valid ? packed : -1);
+	const bool keep = valid && (same & vmask & below) == 0;
+	const unsigned kmask = __ballot_sync(kFull, keep);
+	if (keep) s_list[__popc(kmask & below)] = packed;
+	__syncwarp();
+	const int n = __popc(kmask);
+	mycand = (lane < n) ? s_list[lane] : 0;
+	__syncwarp();
+	return n;
+}
+
+// Shared memory of the PatchMatch kernels: per-tap weights, then per warp a
+// target window (rows x L float4) and a candidate list (32 ints).
+struct PmSmem {
+	float *w;
+	float4 *t;
+	int *list;
+};
+
+__device__ __forceinline__ PmSmem pm_smem(const DistArgs &a, const PmArgs &p)
+{
+	extern __shared__ float4 s_pm[];
+	const int warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+	PmSmem m;
+	const int ws = pm_weight_slots(a.px * a.py);
+	m.w = reinterpret_cast<float *>(s_pm);
+	m.t = s_pm + ws + warp * p.rows * p.L;
+	m.list = reinterpret_cast<int *>(s_pm + ws + warps * p.rows * p.L) + warp * 32;
+	return m;
+}
+
+template <int KIND, int C, int P>
+__global__ void __launch_bounds__(1024, 1) k_pm_init(DistArgs a, PmArgs p, const int2 *__restrict__ init,
+                                                      int2 *__restrict__ nnf, float *__restrict__ dist,
+                                                      unsigned long long *counter)
+{
+	const int lane = threadIdx.x & 31;
+	const PmSmem m = pm_smem(a, p);
+	load_weights(a, m.w);
 	unsigned evals = 0, partial = 0;
 	// block b takes the contiguous range [b * chunk, (b + 1) * chunk) of the
 	// raster-ordered target list, its warps interleaved over the range, so
@@ -279,16 +407,15 @@ __global__ void __launch_bounds__(pm_block<NT>(), NT > 3 ? 2 : 1) k_pm_init(Dist
 			}
 		}
 		float d = FLT_MAX;
+		int2 best = make_int2(-1, -1);
 		if (src_ok(p, n.x, n.y) && tgt_patch_inside(p, x, y)) {
-			TargetPatch<KIND, C, NT> P = warp_target_slot<KIND, C, NT>();
-			load_target<KIND, C, NT>(T, p, pix, P);
-			d = warp_distance<KIND, C, NT>(T, P, p, n.y * p.sW + n.x, FLT_MAX, partial);
+			load_window<C>(p, m.w, x, y, m.t);
+			eval_candidates<KIND, C, P>(p, m.w, m.t, n.x | (n.y << 16), 1, best, d, partial);
 			evals++;
-		} else {
-			n = make_int2(-1, -1);
+			__syncwarp();
 		}
 		if (lane == 0) {
-			nnf[pix] = n;
+			nnf[pix] = best;
 			dist[pix] = d;
 		}
 	}
@@ -298,20 +425,18 @@ __global__ void __launch_bounds__(pm_block<NT>(), NT > 3 ? 2 : 1) k_pm_init(Dist
 	}
 }
 
-template <int KIND, int C, int NT>
-__global__ void __launch_bounds__(pm_block<NT>(), NT > 3 ? 2 : 1) k_pm_sweep(DistArgs a, PmArgs p, int sweep, int jump,
-                                                     const int2 *__restrict__ nnf_in, const float *__restrict__ dist_in,
-                                                     int2 *__restrict__ nnf_out, float *__restrict__ dist_out,
-                                                     unsigned long long *counter)
+template <int KIND, int C, int P>
+__global__ void __launch_bounds__(1024, 1) k_pm_sweep(DistArgs a, PmArgs p, int sweep, int jump,
+                                                       const int2 *__restrict__ nnf_in, const float *__restrict__ dist_in,
+                                                       int2 *__restrict__ nnf_out, float *__restrict__ dist_out,
+                                                       unsigned long long *counter)
 {
 	const int lane = threadIdx.x & 31;
-	TapTable<NT> T;
-	make_taps<KIND, NT>(a, p, T);
+	const PmSmem m = pm_smem(a, p);
+	load_weights(a, m.w);
 	unsigned evals = 0, partial = 0;
-	// block b takes the contiguous range [b * chunk, (b + 1) * chunk) of the
-	// raster-ordered target list, its warps interleaved over the range, so
-	// the warps of an SM work on neighbouring points and share source
-	// neighbourhoods in L1
+	// number of random-search windows: max_window, max_window / 2, ..., 1
+	const int windows = 32 - __clz(p.max_window);
 	const int chunk = (p.nt + gridDim.x - 1) / gridDim.x;
 	const int end = min(p.nt, (int)(blockIdx.x + 1) * chunk);
 	for (int wi = blockIdx.x * chunk + (threadIdx.x >> 5); wi < end; wi += blockDim.x >> 5) {
@@ -320,56 +445,53 @@ __global__ void __launch_bounds__(pm_block<NT>(), NT > 3 ? 2 : 1) k_pm_sweep(Dis
 		int2 best = nnf_in[pix];
 		float bd = dist_in[pix];
 		if (tgt_patch_inside(p, x, y)) {
-			TargetPatch<KIND, C, NT> P = warp_target_slot<KIND, C, NT>();
-			load_target<KIND, C, NT>(T, p, pix, P);
-			auto consider = [&](int cx, int cy) {
-				if ((cx != best.x || cy != best.y) && src_ok(p, cx, cy)) {
-					const float d = warp_distance<KIND, C, NT>(T, P, p, cy * p.sW + cx, bd, partial);
-					evals++;
-					if (d < bd) {
-						bd = d;
-						best = make_int2(cx, cy);
+			load_window<C>(p, m.w, x, y, m.t);
+			// propagation: lane 4s + k proposes the match of neighbour k
+			// (left, right, up, down) at distance 1 (s = 0) or at the jump
+			// distance (s = 1), shifted back by the neighbour's offset
+			bool valid = false;
+			int packed = 0;
+			if (lane < (jump > 1 ? 8 : 4)) {
+				const int s = (lane < 4) ? 1 : jump, k = lane & 3;
+				const int nx = x + ((k == 0) ? -s : (k == 1) ? s : 0);
+				const int ny = y + ((k == 2) ? -s : (k == 3) ? s : 0);
+				if (tgt_ok(p, nx, ny)) {
+					const int2 q = nnf_in[ny * p.tW + nx];
+					if (q.x >= 0) {
+						const int cx = q.x + (x - nx), cy = q.y + (y - ny);
+						valid = src_ok(p, cx, cy);
+						packed = cx | (cy << 16);
 					}
 				}
-			};
-			// propagation from the neighbours at distance 1 and at the jump distance
-#pragma unroll 1
-			for (int si = 0; si < (jump > 1 ? 2 : 1); si++) {
-				const int s = si ? jump : 1;
-				if (tgt_ok(p, x - s, y)) {
-					const int2 q = nnf_in[pix - s];
-					if (q.x >= 0) consider(q.x + s, q.y);
-				}
-				if (tgt_ok(p, x + s, y)) {
-					const int2 q = nnf_in[pix + s];
-					if (q.x >= 0) consider(q.x - s, q.y);
-				}
-				if (tgt_ok(p, x, y - s)) {
-					const int2 q = nnf_in[pix - s * p.tW];
-					if (q.x >= 0) consider(q.x, q.y + s);
-				}
-				if (tgt_ok(p, x, y + s)) {
-					const int2 q = nnf_in[pix + s * p.tW];
-					if (q.x >= 0) consider(q.x, q.y - s);
-				}
 			}
-			// random search around the match after propagation
-			Rng rng(p.key, (uint32_t)pix, (uint32_t)sweep);
-			const int cx = best.x, cy = best.y;
+			int mycand;
+			int n = compact_candidates(valid, packed, best, m.list, mycand);
+			evals += n;
+			eval_candidates<KIND, C, P>(p, m.w, m.t, mycand, n, best, bd, partial);
+			// random search around the match after propagation: lane k draws
+			// in window max_window >> k from its own stream, up to `shots`
+			// draws, and proposes the first that lands in the source
+			valid = false;
+			if (lane < windows) {
+				const int w = p.max_window >> lane;
+				const int x_min = max(best.x - w, 0), y_min = max(best.y - w, 0);
+				const int x_max = min(best.x + w + 1, p.sW), y_max = min(best.y + w + 1, p.sH);
+				Rng rng(p.key, (uint32_t)pix, (uint32_t)sweep, (uint32_t)lane);
 #pragma unroll 1
-			for (int w = p.max_window; w >= 1; w /= 2) {
-				const int x_min = max(cx - w, 0), y_min = max(cy - w, 0);
-				const int x_max = min(cx + w + 1, p.sW), y_max = min(cy + w + 1, p.sH);
-#pragma unroll 1
-				for (int k = 0; k < p.shots; k++) {
+				for (int t = 0; t < p.shots; t++) {
 					const int rx = x_min + rng.below(x_max - x_min);
 					const int ry = y_min + rng.below(y_max - y_min);
 					if (src_ok(p, rx, ry)) {
-						consider(rx, ry);
+						valid = true;
+						packed = rx | (ry << 16);
 						break;
 					}
 				}
 			}
+			n = compact_candidates(valid, packed, best, m.list, mycand);
+			evals += n;
+			eval_candidates<KIND, C, P>(p, m.w, m.t, mycand, n, best, bd, partial);
+			__syncwarp();
 		} else {
 			best = make_int2(-1, -1);
 			bd = FLT_MAX;
@@ -427,30 +549,25 @@ static int jump_for(int sweep, int tW, int tH)
 	return j;
 }
 
-template <int KIND, int C, int NT>
+template <int KIND, int C, int P>
 static void run_sweeps(nli_ctx *ctx, const DistArgs &a, const PmArgs &p, int iterations, const int2 *init,
                        int2 *nnf_x, float *dist_x, int2 *nnf_y, float *dist_y, unsigned long long *counter)
 {
-	// persistent: one block per SM (fewer when there are fewer points)
-	const int block = pm_block<NT>();
-	const int grid = (int)std::min<size_t>(((size_t)p.nt * 32 + block - 1) / block,
-	                                       (size_t)ctx->num_sms * (NT > 3 ? 2 : 1));
-	const size_t smem = target_smem_bytes<KIND, C, NT>(block / 32);
-	static bool smem_attr = false;
-	if (!smem_attr) {
-		NLI_CUDA(cudaFuncSetAttribute(k_pm_init<KIND, C, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-		NLI_CUDA(cudaFuncSetAttribute(k_pm_sweep<KIND, C, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-		smem_attr = true;
-	}
+	// persistent: one 32-warp block per SM (fewer when there are fewer points)
+	const int block = 1024;
+	const int grid = (int)std::min<size_t>(((size_t)p.nt * 32 + block - 1) / block, (size_t)ctx->num_sms);
+	const size_t smem = pm_smem_bytes(a.px * a.py, p.rows, p.L, block / 32);
+	NLI_CUDA(cudaFuncSetAttribute(k_pm_init<KIND, C, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	NLI_CUDA(cudaFuncSetAttribute(k_pm_sweep<KIND, C, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	{
 		ProfScope ps(ctx, "pm_init");
-		k_pm_init<KIND, C, NT><<<grid, block, smem, ctx->stream>>>(a, p, init, nnf_x, dist_x, counter);
+		k_pm_init<KIND, C, P><<<grid, block, smem, ctx->stream>>>(a, p, init, nnf_x, dist_x, counter);
 		NLI_CHECK_LAUNCH();
 	}
 	for (int it = 0; it < iterations; it++) {
 		const bool even = (it % 2) == 0;
 		ProfScope ps(ctx, "pm_sweep");
-		k_pm_sweep<KIND, C, NT><<<grid, block, smem, ctx->stream>>>(
+		k_pm_sweep<KIND, C, P><<<grid, block, smem, ctx->stream>>>(
 		    a, p, it, jump_for(it, p.tW, p.tH), even ? nnf_x : nnf_y, even ? dist_x : dist_y, even ? nnf_y : nnf_x,
 		    even ? dist_y : dist_x, counter);
 		NLI_CHECK_LAUNCH();
@@ -464,20 +581,17 @@ void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patch
 {
 	DistArgs a;
 	fill_dist_args(a, dp, C);
-	NLI_REQUIRE(C == 1 || C == 3 || C == 4, NLI_E_UNSUPPORTED, "PatchMatch kernels cover 1, 3 or 4 channels");
+	NLI_REQUIRE(sW < 32768 && sH < 32768, NLI_E_UNSUPPORTED, "PatchMatch source sides must be below 32768");
 	cudaStream_t s = ctx->stream;
-	const int nS = sW * sH, nT = tW * tH;
+	const int nT = tW * tH;
 
-	// packed features (gradients included) of source and target
-	float4 *fs4 = ctx->buf<float4>("pm.fs4", (size_t)nS * a.p4);
-	float *fs1 = a.f1 ? ctx->buf<float>("pm.fs1", (size_t)nS) : nullptr;
-	launch_features(s, dp.kind, src, sW, sH, C, fs4, fs1);
-	float4 *ft4 = fs4;
-	float *ft1 = fs1;
+	// padded float4 pixels of source and target
+	float4 *s4 = ctx->buf<float4>("pm.src4", (size_t)(sW + 1) * (sH + 1));
+	launch_pad4(s, src, sW, sH, C, s4);
+	float4 *t4 = s4;
 	if (!(tgt == src && tW == sW && tH == sH)) {
-		ft4 = ctx->buf<float4>("pm.ft4", (size_t)nT * a.p4);
-		ft1 = a.f1 ? ctx->buf<float>("pm.ft1", (size_t)nT) : nullptr;
-		launch_features(s, dp.kind, tgt, tW, tH, C, ft4, ft1);
+		t4 = ctx->buf<float4>("pm.tgt4", (size_t)(tW + 1) * (tH + 1));
+		launch_pad4(s, tgt, tW, tH, C, t4);
 	}
 
 	if (!tlist) {
@@ -485,7 +599,6 @@ void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patch
 		n_target = compact_mask(ctx, tmask, tW, tH, l, "pm");
 		tlist = l;
 	}
-
 	const int2 *init = reinterpret_cast<const int2 *>(init_nnf);
 	if (init_nnf && init_nnf == out_nnf) {
 		int2 *copy = ctx->buf<int2>("pm.init_copy", nT);
@@ -502,12 +615,10 @@ void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patch
 	NLI_CHECK_LAUNCH();
 	if (n_target > 0) {
 		PmArgs p;
-		p.fs4 = fs4;
-		p.fs1 = fs1;
-		p.ft4 = ft4;
-		p.ft1 = ft1;
-		p.sN = nS;
-		p.tN = nT;
+		p.src = s4;
+		p.tgt = t4;
+		p.sWp = sW + 1;
+		p.tWp = tW + 1;
 		p.smask = smask;
 		p.tmask = tmask;
 		p.tlist = tlist;
@@ -522,28 +633,39 @@ void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patch
 		p.ry = a.ry;
 		p.ex = a.px - a.rx;
 		p.ey = a.py - a.ry;
+		const bool grad = dp.kind == NLI_DIST_L2_COMBINED || dp.kind == NLI_DIST_L2_RGBD;
+		p.L = a.px + (grad ? 1 : 0);
+		p.K = 32 / p.L;
+		p.rows = a.py + (grad ? 1 : 0);
+		p.lambda = a.lambda;
+		p.lambda_d = a.lambda_d;
 		const uint64_t call = ctx->call_counter++;
 		const uint64_t k = ctx->seed ^ (call * 0x9E3779B97F4A7C15ULL);
 		p.key = make_uint2((uint32_t)k, (uint32_t)(k >> 32) ^ (uint32_t)call);
 		if (energy) NLI_CUDA(cudaMemsetAsync(counter, 0, 2 * sizeof(unsigned long long), s));
-#define NLI_PM_CASE(KIND, CC)                                                                              \
-	if (dp.kind == KIND && C == CC) {                                                                          \
-		if (a.px * a.py <= 96)                                                                                 \
-			run_sweeps<KIND, CC, 3>(ctx, a, p, pm.iterations, init, nnf_x, dist_x, nnf_y, dist_y, counter);  \
-		else                                                                                                   \
-			run_sweeps<KIND, CC, 8>(ctx, a, p, pm.iterations, init, nnf_x, dist_x, nnf_y, dist_y, counter);  \
-		handled = true;                                                                                        \
+		// 9 x 9 patches (the reference's default) have their rows unrolled
+		const bool p9 = a.px == 9 && a.py == 9;
+#define NLI_PM_CASE(KIND, CC)                                                                                \
+	if (dp.kind == KIND && C == CC) {                                                                            \
+		if (p9)                                                                                                  \
+			run_sweeps<KIND, CC, 9>(ctx, a, p, pm.iterations, init, nnf_x, dist_x, nnf_y, dist_y, counter); \
+		else                                                                                                     \
+			run_sweeps<KIND, CC, 0>(ctx, a, p, pm.iterations, init, nnf_x, dist_x, nnf_y, dist_y, counter); \
+		handled = true;                                                                                          \
 	}
 		bool handled = false;
 		NLI_PM_CASE(NLI_DIST_L2_COMBINED, 3)
 		NLI_PM_CASE(NLI_DIST_L2_COMBINED, 1)
+		NLI_PM_CASE(NLI_DIST_L2_COMBINED, 2)
 		NLI_PM_CASE(NLI_DIST_L2_COMBINED, 4)
 		NLI_PM_CASE(NLI_DIST_L2_RGBD, 4)
 		NLI_PM_CASE(NLI_DIST_L2_NORM, 3)
 		NLI_PM_CASE(NLI_DIST_L2_NORM, 1)
+		NLI_PM_CASE(NLI_DIST_L2_NORM, 2)
 		NLI_PM_CASE(NLI_DIST_L2_NORM, 4)
 		NLI_PM_CASE(NLI_DIST_L1_NORM, 3)
 		NLI_PM_CASE(NLI_DIST_L1_NORM, 1)
+		NLI_PM_CASE(NLI_DIST_L1_NORM, 2)
 		NLI_PM_CASE(NLI_DIST_L1_NORM, 4)
 #undef NLI_PM_CASE
 		NLI_REQUIRE(handled, NLI_E_UNSUPPORTED, "no PatchMatch kernel for this distance / channel count");

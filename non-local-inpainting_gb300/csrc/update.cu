@@ -528,8 +528,12 @@ __global__ void __launch_bounds__(kCgBlock) k_poisson_cg(PoissonArgs a, const Un
 	if (threadIdx.x == 0) diff_part[blockIdx.x] = dacc;
 }
 
-// Conjugate gradient on one thread-block cluster with every vector and the
-// system itself in shared memory.
+// Conjugate gradient on thread-block clusters with every vector and the
+// system itself in shared memory.  Cluster g of the grid solves channels
+// [g * C, (g + 1) * C) of the Ctot-channel image; the channels are
+// independent systems (the reference solves them one after the other), so
+// one cluster per channel (C = 1) spreads the solve over more SMs and lets
+// each channel stop at its own convergence.
 //
 // CTA `rank` of the cluster (up to 16 CTAs of 512 threads) owns the
 // contiguous unknown range [rank * chunk, (rank + 1) * chunk), chunk <=
@@ -584,6 +588,7 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
                          const float *__restrict__ x0, int *__restrict__ iters_out, const int32_t *__restrict__ hole,
                          const float *orig, float *img, double *__restrict__ diff_part)
 {
+	const int Ctot = a.C;
 	namespace cgs = cooperative_groups;
 	cgs::cluster_group cluster = cgs::this_cluster();
 	extern __shared__ float smem[];
@@ -593,6 +598,9 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 	__shared__ int s_active[4];
 	__shared__ float *base[3][kClusterMax];  // r, dA, dB of every CTA
 	const int rank = (int)cluster.block_rank(), ncta = (int)cluster.num_blocks();
+	const int group = (int)blockIdx.x / ncta, cb = group * C;  // this cluster's first channel
+	b += (size_t)cb * a.nh;
+	x0 += (size_t)cb * a.nh;
 	const int nh = a.nh;
 	const int lo = rank * chunk, own = max(0, min(nh, lo + chunk) - lo);
 	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -663,7 +671,7 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 #pragma unroll
 			for (int j = 0; j < 4; j++)
 				if (gk[j] >= 0) lap += coefs[j] * xc[gk[j]];
-			const float rv = b[(size_t)c * nh + k] - (a.lambda[c] * n.S * xk - (1.0f - a.lambda[c]) * lap);
+			const float rv = b[(size_t)c * nh + k] - (a.lambda[cb + c] * n.S * xk - (1.0f - a.lambda[cb + c]) * lap);
 			s_r[(size_t)l * C + c] = rv;
 			s_dA[(size_t)l * C + c] = 0.f;
 			s_x[(size_t)l * C + c] = xk;
@@ -719,7 +727,7 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 #pragma unroll
 				for (int j = 0; j < 4; j++)
 					if (codes[j] != kNoNb) lap += coefs[j] * (nr_[j][c] + beta[c] * nd_[j][c]);
-				const float qv = a.lambda[c] * n.S * dk - (1.0f - a.lambda[c]) * lap;
+				const float qv = a.lambda[cb + c] * n.S * dk - (1.0f - a.lambda[cb + c]) * lap;
 				dnew[o] = dk;
 				q[u][c] = qv;
 				facc[c] = fmaf(rk, qv, facc[c]);
@@ -776,23 +784,23 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 		__syncthreads();
 		h = 1 - h;
 	}
-	if (rank == 0 && threadIdx.x < C) iters_out[threadIdx.x] = it[threadIdx.x];
+	if (rank == 0 && threadIdx.x < C) iters_out[cb + threadIdx.x] = it[threadIdx.x];
 	// u = orig + delta on the hole (:89-104)
 	double dacc = 0.0;
 	for (int l = threadIdx.x; l < own; l += blockDim.x) {
 		const int pix = hole[lo + l];
 #pragma unroll
 		for (int c = 0; c < C; c++) {
-			const float o = orig[(size_t)C * pix + c];
+			const float o = orig[(size_t)Ctot * pix + cb + c];
 			const float v = o + s_x[(size_t)l * C + c];
-			const float prev = img[(size_t)C * pix + c];
+			const float prev = img[(size_t)Ctot * pix + cb + c];
 			const float dd = prev - v;
 			dacc += (double)(dd * dd);
-			img[(size_t)C * pix + c] = v;
+			img[(size_t)Ctot * pix + cb + c] = v;
 		}
 	}
 	dacc = block_sum<kClusterBlock>(dacc, &red[0][0]);
-	if (threadIdx.x == 0) diff_part[rank] = dacc;
+	if (threadIdx.x == 0) diff_part[group * ncta + rank] = dacc;
 	cluster.sync();  // no CTA leaves while others may still read its shared memory
 }
 
@@ -890,7 +898,7 @@ static void poisson_run(nli_ctx *ctx, const UpdArgs &u, const nli_update_params 
 	if (ctx->cg_cluster_max >= 1) {
 		ncta = std::max(1, std::min(ctx->cg_cluster_max, (nh + 2 * kClusterBlock - 1) / (2 * kClusterBlock)));
 		chunk = (nh + ncta - 1) / ncta;
-		if ((size_t)kClusterVectors * C * chunk * sizeof(float) + chunk * sizeof(UnkC) > kSmemBudget ||
+		if ((size_t)kClusterVectors * chunk * sizeof(float) + chunk * sizeof(UnkC) > kSmemBudget ||
 		    chunk > kClusterMaxChunk)
 			ncta = chunk = 0;
 	}
@@ -903,14 +911,15 @@ static void poisson_run(nli_ctx *ctx, const UpdArgs &u, const nli_update_params 
 	int *iters = ctx->buf<int>("poi.iters", 4);
 	const float *orig_c = orig;
 	if (ncta > 0) {
-		const size_t smem = (size_t)kClusterVectors * C * chunk * sizeof(float) + chunk * sizeof(UnkC);
+		// one cluster per channel
+		const size_t smem = (size_t)kClusterVectors * chunk * sizeof(float) + chunk * sizeof(UnkC);
 		UnkC *unkc = ctx->buf<UnkC>("poi.unkc", nh);
 		k_poisson_compact<<<(nh + 255) / 256, 256, 0, s>>>(unk, nh, chunk, unkc);
 		NLI_CHECK_LAUNCH();
 		{
-			double *diff_part = ctx->buf<double>("poi.diff", ncta + 1);
+			double *diff_part = ctx->buf<double>("poi.diff", (size_t)C * ncta + 1);
 			cudaLaunchConfig_t cfg = {};
-			cfg.gridDim = dim3(ncta);
+			cfg.gridDim = dim3(C * ncta);
 			cfg.blockDim = dim3(kClusterBlock);
 			cfg.dynamicSmemBytes = smem;
 			cfg.stream = s;
@@ -922,10 +931,10 @@ static void poisson_run(nli_ctx *ctx, const UpdArgs &u, const nli_update_params 
 			cfg.attrs = attr;
 			cfg.numAttrs = 1;
 			ProfScope ps(ctx, "poisson_cg");
-			NLI_CUDA(cudaLaunchKernelEx(&cfg, cluster_kernel(C), pa, chunk, (const UnkC *)unkc, (const float *)b,
+			NLI_CUDA(cudaLaunchKernelEx(&cfg, cluster_kernel(1), pa, chunk, (const UnkC *)unkc, (const float *)b,
 			                            (const float *)x, iters, hole, orig_c, image, diff_part));
 			nli_count_launch_internal();
-			*n_partials = ncta;
+			*n_partials = C * ncta;
 			return;
 		}
 	}
