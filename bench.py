@@ -49,7 +49,9 @@ CG_BYTES_PER_UNKNOWN_ITER = 32
 L2_FLUSH_BYTES = 256 << 20
 COUNTS = os.path.join(ROOT, "tests", "golden", "config2_reference_counts.json")
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
-TRAFFIC = os.path.join(ROOT, "profiles", "pm_sweep_traffic.json")
+# ncu summary of the dominant kernel; its "traffic_bytes_per_launch:" line is
+# the DRAM bytes (read + write) of one finest-scale sweep
+TRAFFIC = os.path.join(ROOT, "profiles", "pm_sweep_l2combined_512x512.md")
 
 
 def workload_desc():
@@ -302,11 +304,14 @@ def run_ours(args):
     pm_launches = sum(v[0] for k, v in prof.items() if k.startswith("pm_"))
     traffic = None
     if os.path.exists(TRAFFIC):
-        traffic = json.load(open(TRAFFIC)).get("bytes_per_launch")
+        import re
+        m = re.search(r"traffic_bytes_per_launch:\s*(\d+)", open(TRAFFIC).read())
+        traffic = int(m.group(1)) if m else None
     pm_tflops = cand * FLOP_PER_CANDIDATE / (pm_ms / 1e3) / 1e12 if pm_ms > 0 else 0.0
     roofline = {"kernel": "k_pm_init + k_pm_sweep (PatchMatch)", "bound": "fp32", "achieved": pm_tflops,
                 "peak": fp32_peak, "unit": "TFLOP/s", "frac": pm_tflops / fp32_peak if fp32_peak else None,
-                "traffic": traffic, "launches": pm_launches, "ms": pm_ms,
+                "traffic": traffic, "traffic_scope": "ncu DRAM bytes of one finest-scale (512x512) sweep launch",
+                "launches": pm_launches, "ms": pm_ms,
                 "peak_source": "nominal FP32 (%d SMs x 128 lanes x 2 FLOP) at the sampled median SM clock %.0f MHz; "
                                "MEASURED_PEAKS.json has no FP32 figure" % (n_sm, sm_mhz),
                 "flop_per_candidate": FLOP_PER_CANDIDATE, "candidates": cand}

@@ -215,16 +215,43 @@ __global__ void k_dt_columns(const uint8_t *__restrict__ mask, int W, int H, flo
 {
 	const int x = blockIdx.x * blockDim.x + threadIdx.x;
 	if (x >= W) return;
-	g[x] = mask[x] ? INF : 0.0f;
-	for (int y = 1; y < H; y++) g[y * W + x] = mask[y * W + x] ? fa(g[(y - 1) * W + x], 1.0f) : 0.0f;
-	for (int y = H - 2; y >= 0; y--)
-		if (g[(y + 1) * W + x] < g[y * W + x]) g[y * W + x] = fa(g[(y + 1) * W + x], 1.0f);
+	float run = mask[x] ? INF : 0.0f;
+	g[x] = run;
+	for (int y = 1; y < H; y++) {
+		run = mask[y * W + x] ? fa(run, 1.0f) : 0.0f;
+		g[y * W + x] = run;
+	}
+	for (int y = H - 2; y >= 0; y--) {
+		const float v = g[y * W + x];
+		if (run < v) {
+			run = fa(run, 1.0f);
+			g[y * W + x] = run;
+		} else {
+			run = v;
+		}
+	}
 }
 
 __device__ __forceinline__ float dt_f(int x, int xi, float gi)
 {
 	const double dx = (double)(float)(x - xi), g = (double)gi;
 	return __double2float_rn(__dsqrt_rn(da(dm(dx, dx), dm(g, g))));
+}
+
+// dt_f(x, i, gi) > dt_f(x, u, gu), decided without square roots where that
+// is exact.  Both squares (x - i)^2 + gi^2 are integers (gi holds an integer
+// column distance).  Below 2^21 the square roots of two different integers
+// are more than 2 float ulps apart, so their float roundings (through
+// double, each within half an ulp) keep the order of the integers; above
+// it the rounded roots are
+// compared as the reference compares them.
+__device__ __forceinline__ bool dt_greater(int x, int i, float gi, int u, float gu)
+{
+	const double dxi = (double)(float)(x - i), dxu = (double)(float)(x - u);
+	const double a = da(dm(dxi, dxi), dm((double)gi, (double)gi));
+	const double b = da(dm(dxu, dxu), dm((double)gu, (double)gu));
+	if (a < 2097152.0 && b < 2097152.0) return a > b;
+	return dt_f(x, i, gi) > dt_f(x, u, gu);
 }
 
 __device__ __forceinline__ int dt_sep(int i, int u, float gi, float gu)
@@ -247,7 +274,7 @@ __global__ void k_dt_rows(const float *__restrict__ g, int W, int H, int *__rest
 	s[0] = 0;
 	t[0] = 0;
 	for (int u = 1; u < W; u++) {
-		while (q >= 0 && dt_f(t[q], s[q], gy[s[q]]) > dt_f(t[q], u, gy[u])) q--;
+		while (q >= 0 && dt_greater(t[q], s[q], gy[s[q]], u, gy[u])) q--;
 		if (q < 0) {
 			q = 0;
 			s[0] = u;
@@ -272,9 +299,10 @@ void distance_transform_run(nli_ctx *ctx, const uint8_t *mask, int W, int H, flo
 	int *sb = ctx->buf<int>("dt.s", (size_t)W * H);
 	int *tb = ctx->buf<int>("dt.t", (size_t)W * H);
 	const float INF = (float)((unsigned)W + (unsigned)H);
-	k_dt_columns<<<(W + 127) / 128, 128, 0, ctx->stream>>>(mask, W, H, INF, g);
+	k_dt_columns<<<(W + 31) / 32, 32, 0, ctx->stream>>>(mask, W, H, INF, g);
 	NLI_CHECK_LAUNCH();
-	k_dt_rows<<<(H + 127) / 128, 128, 0, ctx->stream>>>(g, W, H, sb, tb, out);
+	// one row per thread, 32 rows per block: the rows spread over the SMs
+	k_dt_rows<<<(H + 31) / 32, 32, 0, ctx->stream>>>(g, W, H, sb, tb, out);
 	NLI_CHECK_LAUNCH();
 }
 
