@@ -292,6 +292,8 @@ def run_ours(args):
             torch.distributed.destroy_process_group()
         return 0
 
+    batch = None if (args.batch_count <= 0 or world > 1) else batch_compare(pkg, ctx, args, local)
+
     # roofline of the dominant kernel, from the events timed inside the steps
     peaks = json.load(open(PEAKS)) if os.path.exists(PEAKS) else {}
     sm_mhz = clk.get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
@@ -346,6 +348,7 @@ def run_ours(args):
         "kernels": kernels,
         "dominant_kernel": dom[0],
         "cpu_baseline": cpu,
+        "batched": batch,
         "process_stats": {"iterations": list(st.iterations[:p.scales]), "patchmatch_calls": st.patchmatch_calls,
                           "update_calls": st.update_calls, "cg_iterations": st.cg_iterations},
     }
@@ -353,6 +356,60 @@ def run_ours(args):
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0
+
+
+def batch_compare(pkg, ctx, args, local):
+    """Plain per-image path against the batched path on a seeded batch shaped
+    like the uneven-batch workload: `--batch-count` images, sides
+    log-uniform in [128, --batch-max-side], aspect 0.5-2, 5-30 % ellipse or
+    stroke holes, alternating nlmeans / nlpoisson, patch 9, scales
+    |round(log(size 0.1) / log(0.75))| with the automatic coarsest rate.
+    Inputs resident in HBM; each path timed once after one warm-up pass,
+    with CUDA events on the context's stream (the batch joins it)."""
+    import torch
+    from nli_gb300 import workloads as wl
+    items5 = wl.config5(seed=5, count=args.batch_count, max_side=args.batch_max_side)
+    items, params, mpix = [], [], 0.0
+    for img, mask, method, scales in items5:
+        items.append((ctx._f32(img), ctx._u8(mask)))
+        params.append(wl.config5_params(mask, method, scales))
+        mpix += img.shape[0] * img.shape[1] / 1e6
+    outs = [torch.empty_like(i) for i, _ in items]
+    ref = [torch.empty_like(i) for i, _ in items]
+    seed = 2024
+
+    def plain():
+        for i, ((im, m), p) in enumerate(zip(items, params)):
+            ctx.set_seed(ctx.batch_seed(seed, i))
+            ctx.process_device(im, m, p, out=ref[i])
+
+    def batched():
+        ctx.set_seed(seed)
+        ctx.set_batch_width(args.batch_width)
+        ctx.process_batch_device(items, params, outs=outs)
+
+    def timed(fn):
+        torch.cuda.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        fn()
+        b.record()
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / 1e3
+
+    l0 = ctx.launch_count()
+    batched()
+    launches = ctx.launch_count() - l0
+    tb = timed(batched)
+    plain()
+    tp = timed(plain)
+    return {"workload": "uneven batch: %d images, sides log-uniform 128-%d, aspect 0.5-2, 5-30%% ellipse/stroke "
+                        "holes, nlmeans/nlpoisson alternating, patch 9, scales |round(log(0.1 size)/log(0.75))|, "
+                        "automatic coarsest rate (seed 5)" % (len(items), args.batch_max_side),
+            "mpix": mpix, "plain_mpix_s": mpix / tp, "batched_mpix_s": mpix / tb, "speedup": tp / tb,
+            "plain_s": tp, "batched_s": tb, "batch_width": args.batch_width, "gpu_launches": int(launches),
+            "identical_to_plain": all(bool(torch.equal(x, y)) for x, y in zip(outs, ref)),
+            "scales": [p.scales for p in params]}
 
 
 def run_case(args):
@@ -389,6 +446,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch-count", type=int, default=16,
+                    help="images in the batched-vs-plain comparison (0 skips it)")
+    ap.add_argument("--batch-max-side", type=int, default=512)
+    ap.add_argument("--batch-width", type=int, default=8)
     args = ap.parse_args()
     if args.case:
         return run_case(args)

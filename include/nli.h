@@ -296,6 +296,33 @@ int nli_process_device(nli_ctx *ctx, const nli_process_params *params,
                        const float *image, const uint8_t *mask, int W, int H, int C,
                        float *out, nli_process_stats *stats);
 
+/* ---- batched driver ------------------------------------------------------ */
+/* Many independent image/mask pairs on one GPU.  The reference has no batch
+ * entry point: it replaces a host loop of ImageInpainting::process calls
+ * (image_inpainting.cpp:68-190; main.cpp:279 makes one).  Image i has its
+ * own parameters params[i], sizes widths[i] x heights[i] x channels[i] and
+ * buffers images[i], masks[i], outputs[i]; nli_process_batch takes host
+ * pointers (copies inside the call), nli_process_batch_device device
+ * pointers (ordered after the work already queued on the context's stream,
+ * and the stream waits for the batch).  Up to the context's batch width of
+ * images are in flight at once, each on its own stream.  Image i runs
+ * exactly as nli_process after nli_set_seed(ctx, nli_batch_seed(seed, i)),
+ * seed being the context's seed.  stats (n entries) and status (n entries,
+ * the per-image result) may be NULL.  Returns NLI_OK when every image
+ * succeeded, else the status of the first failed image (in index order). */
+int nli_process_batch(nli_ctx *ctx, int n, const nli_process_params *params,
+                      const float *const *images, const uint8_t *const *masks,
+                      const int32_t *widths, const int32_t *heights, const int32_t *channels,
+                      float *const *outputs, nli_process_stats *stats, int32_t *status);
+int nli_process_batch_device(nli_ctx *ctx, int n, const nli_process_params *params,
+                             const float *const *images, const uint8_t *const *masks,
+                             const int32_t *widths, const int32_t *heights, const int32_t *channels,
+                             float *const *outputs, nli_process_stats *stats, int32_t *status);
+/* Images in flight in a batch (default 8, at least 1). */
+int nli_ctx_set_batch_width(nli_ctx *ctx, int width);
+/* The seed image `index` of a batch runs with. */
+uint64_t nli_batch_seed(uint64_t seed, int index);
+
 #ifdef __cplusplus
 }
 #endif

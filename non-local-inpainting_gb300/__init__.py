@@ -89,6 +89,10 @@ def load(path=LIB_PATH):
     proto("nli_update", I, [P, up, P, P, P, P, P, P, I, I, I, ct.POINTER(ct.c_double)])
     proto("nli_process", I, [P, prp, P, P, I, I, I, P, st])
     proto("nli_process_device", I, [P, prp, P, P, I, I, I, P, st])
+    proto("nli_process_batch", I, [P, I, prp, P, P, P, P, P, P, st, P])
+    proto("nli_process_batch_device", I, [P, I, prp, P, P, P, P, P, P, st, P])
+    proto("nli_ctx_set_batch_width", I, [P, I])
+    proto("nli_batch_seed", ct.c_uint64, [ct.c_uint64, I])
     proto("nli_launch_count", ct.c_int64, [])
     proto("nli_ctx_set_profiling", I, [P, I])
     proto("nli_ctx_profile_entry", I, [P, I, ct.c_char_p, I, ct.POINTER(ct.c_int64), ct.POINTER(ct.c_double)])
@@ -327,6 +331,56 @@ class Context:
         self._check(self.lib.nli_process(self.h, ct.byref(params), img.ctypes.data_as(P), mask.ctypes.data_as(P),
                                          W, H, C, out.ctypes.data_as(P), ct.byref(st)))
         return out, st.as_dict()
+
+    def set_batch_width(self, width):
+        """Images in flight at once in process_batch."""
+        self._check(self.lib.nli_ctx_set_batch_width(self.h, width))
+
+    def _batch_arrays(self, items, params, device):
+        n = len(items)
+        pa = (ProcessParams * n)(*params)
+        arr = lambda T, vals: (T * n)(*vals)  # noqa: E731
+        if device:
+            dims = [_dims(img) for img, _ in items]
+            ptr = lambda t: t.data_ptr()  # noqa: E731
+        else:
+            dims = [(img.shape[1], img.shape[0], 1 if img.ndim == 2 else img.shape[2]) for img, _ in items]
+            ptr = lambda a: a.ctypes.data  # noqa: E731
+        return (n, pa, arr(ct.c_void_p, [ptr(i) for i, _ in items]), arr(ct.c_void_p, [ptr(m) for _, m in items]),
+                arr(ct.c_int32, [d[0] for d in dims]), arr(ct.c_int32, [d[1] for d in dims]),
+                arr(ct.c_int32, [d[2] for d in dims]))
+
+    def process_batch(self, items, params):
+        """Many (image, mask) host pairs with one params entry each; returns
+        ([outputs], [stats]).  Image i is computed as process() after
+        set_seed(batch_seed(seed, i))."""
+        items = [(np.ascontiguousarray(i, np.float32), np.ascontiguousarray(m).astype(np.uint8)) for i, m in items]
+        outs = [np.empty_like(i) for i, _ in items]
+        n, pa, ims, ms, ws, hs, cs = self._batch_arrays(items, params, False)
+        op = (ct.c_void_p * n)(*[o.ctypes.data for o in outs])
+        st = (ProcessStats * n)()
+        status = (ct.c_int32 * n)()
+        rc = self.lib.nli_process_batch(self.h, n, pa, ims, ms, ws, hs, cs, op, st, status)
+        self.last_batch_status = list(status)
+        self._check(rc)
+        return outs, [s.as_dict() for s in st]
+
+    def process_batch_device(self, items, params, outs=None):
+        """process_batch on device tensors; returns ([outputs], [stats])."""
+        items = [(self._f32(i), self._u8(m)) for i, m in items]
+        if outs is None:
+            outs = [self.torch.empty_like(i) for i, _ in items]
+        n, pa, ims, ms, ws, hs, cs = self._batch_arrays(items, params, True)
+        op = (ct.c_void_p * n)(*[o.data_ptr() for o in outs])
+        st = (ProcessStats * n)()
+        status = (ct.c_int32 * n)()
+        rc = self.lib.nli_process_batch_device(self.h, n, pa, ims, ms, ws, hs, cs, op, st, status)
+        self.last_batch_status = list(status)
+        self._check(rc)
+        return outs, [s.as_dict() for s in st]
+
+    def batch_seed(self, seed, index):
+        return int(self.lib.nli_batch_seed(seed, index))
 
     def process_device(self, img, mask, params, out=None):
         """ImageInpainting::process on device tensors; returns (out, stats)."""

@@ -14,7 +14,8 @@ LIB = os.path.join(HERE, "libnli_gb300.so")
 DROPIN = os.path.join(HERE, "libnli_dropin.so")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
-SOURCES = ["api.cu", "gradient.cu", "distance.cu", "patchmatch.cu", "update.cu", "pyramid.cu", "process.cu"]
+SOURCES = ["api.cu", "gradient.cu", "distance.cu", "patchmatch.cu", "update.cu", "pyramid.cu", "process.cu",
+           "batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", os.path.join(ROOT, "include"), "-I", CSRC]

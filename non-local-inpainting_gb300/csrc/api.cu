@@ -165,6 +165,8 @@ int nli_ctx_destroy(nli_ctx *ctx)
 	if (!ctx) return NLI_E_INVALID;
 	cudaSetDevice(ctx->device);
 	cudaStreamSynchronize(ctx->stream);
+	for (nli_ctx *w : ctx->workers) nli_ctx_destroy(w);
+	ctx->workers.clear();
 	for (auto &kv : ctx->bufs) kv.second.release();
 	if (ctx->status) cudaFree(ctx->status);
 	if (ctx->host_pinned) cudaFreeHost(ctx->host_pinned);
@@ -394,5 +396,42 @@ int nli_process(nli_ctx *ctx, const nli_process_params *params, const float *ima
 	NLI_CUDA(cudaStreamSynchronize(ctx->stream));
 	API_END(ctx)
 }
+
+static void require_batch(int n, const void *params, const void *images, const void *masks, const void *widths,
+                          const void *heights, const void *channels, const void *outputs)
+{
+	NLI_REQUIRE(n >= 0, NLI_E_INVALID, "negative batch size");
+	if (n > 0) require_ptrs({params, images, masks, widths, heights, channels, outputs});
+}
+
+int nli_process_batch(nli_ctx *ctx, int n, const nli_process_params *params, const float *const *images,
+                      const uint8_t *const *masks, const int32_t *widths, const int32_t *heights,
+                      const int32_t *channels, float *const *outputs, nli_process_stats *stats, int32_t *status)
+{
+	API_BEGIN(ctx)
+	require_batch(n, params, images, masks, widths, heights, channels, outputs);
+	process_batch_run(ctx, n, params, images, masks, widths, heights, channels, outputs, stats, status, true);
+	API_END(ctx)
+}
+
+int nli_process_batch_device(nli_ctx *ctx, int n, const nli_process_params *params, const float *const *images,
+                             const uint8_t *const *masks, const int32_t *widths, const int32_t *heights,
+                             const int32_t *channels, float *const *outputs, nli_process_stats *stats,
+                             int32_t *status)
+{
+	API_BEGIN(ctx)
+	require_batch(n, params, images, masks, widths, heights, channels, outputs);
+	process_batch_run(ctx, n, params, images, masks, widths, heights, channels, outputs, stats, status, false);
+	API_END(ctx)
+}
+
+int nli_ctx_set_batch_width(nli_ctx *ctx, int width)
+{
+	if (!ctx || width < 1) return NLI_E_INVALID;
+	ctx->batch_width = width;
+	return NLI_OK;
+}
+
+uint64_t nli_batch_seed(uint64_t seed, int index) { return batch_seed(seed, index); }
 
 }  // extern "C"

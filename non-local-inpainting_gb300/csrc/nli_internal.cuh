@@ -107,6 +107,9 @@ struct nli_ctx {
 	};
 	bool profiling = false;
 	std::map<std::string, ProfEntry> prof;
+	// batched processing (batch.cu): images in flight and their worker contexts
+	int batch_width = 8;
+	std::vector<nli_ctx *> workers;
 	std::vector<cudaEvent_t> event_pool;
 
 	cudaEvent_t take_event()
@@ -228,6 +231,13 @@ void scale_masks_run(nli_ctx *ctx, const uint8_t *ext, int W, int H, int margin,
                      uint8_t *tgt, int *empty_dev);
 void poisson_init_run(nli_ctx *ctx, float *img, const uint8_t *mask, int W, int H, int C);
 int sample_size_host(unsigned size, float factor);
+
+// batch.cu
+uint64_t batch_seed(uint64_t seed, int index);
+void process_batch_run(nli_ctx *ctx, int n, const nli_process_params *params, const float *const *images,
+                       const uint8_t *const *masks, const int32_t *widths, const int32_t *heights,
+                       const int32_t *channels, float *const *outputs, nli_process_stats *stats, int32_t *status,
+                       bool host_buffers);
 
 // process.cu
 void process_run(nli_ctx *ctx, const nli_process_params &p, const float *img, const uint8_t *mask, int W,

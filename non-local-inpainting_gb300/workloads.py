@@ -226,3 +226,25 @@ def config5(seed=0, count=64, min_side=128, max_side=1024):
         scales = abs(int(round(math.log(min(w, h) * 0.1) / math.log(0.75))))
         items.append((img, mask, method, max(scales, 1)))
     return items
+
+
+def coarsest_rate_auto(mask, patch=9):
+    """The CLI's rule for -coarse 0 (main.cpp:166-177): coarsest rate =
+    min(1.5 * patch / max distance to the hole boundary, 1), in float."""
+    from scipy.ndimage import distance_transform_edt
+    d = distance_transform_edt(np.asarray(mask) != 0)
+    max_dist = np.float32(d.max()) if d.size else np.float32(0)
+    if max_dist <= 0:
+        return 1.0
+    r = np.float32(1.5) * np.float32(patch) / max_dist
+    return float(min(r, np.float32(1.0)))
+
+
+def config5_params(mask, method, scales, iters=200):
+    """Parameters of one batch item: the CLI defaults for `method`, the
+    automatic coarsest rate, and one scale when that rate is 1 (main.cpp:199-202)."""
+    coarse = coarsest_rate_auto(mask)
+    if abs(coarse - 1.0) < 1e-5:
+        scales = 1
+    return params(method, scales=scales, coarse=coarse, iters=iters)
+
