@@ -156,6 +156,23 @@ def cpu_sample(img, mask, p, iterations):
     return est, wall, orc.max_threads
 
 
+def max_over_ranks(value, device="cpu"):
+    """The largest `value` over the ranks of the default process group (the
+    value itself with one rank): the job's time is its slowest rank's."""
+    import torch
+    if not (torch.distributed.is_available() and torch.distributed.is_initialized()):
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(world, steps, mpix_per_rank_step, total_ms):
+    """Whole-job Mpix/s: every rank processes its own images (replicas), so
+    the units of all ranks divide the slowest rank's time."""
+    return world * steps * mpix_per_rank_step / (total_ms / 1e3)
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -257,12 +274,8 @@ def run_ours(args):
     ctx.set_profiling(False)
     launches = ctx.launch_count() - l0
     c1 = ctx.counters()
-    total_ms = sum(ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * args.steps * mpix / (total_ms / 1e3)
+    total_ms = max_over_ranks(sum(ms), dev)
+    value = job_throughput(world, args.steps, mpix, total_ms)
 
     # end to end: pinned host buffers, copies inside the timed region
     import ctypes as ct
@@ -280,12 +293,8 @@ def run_ours(args):
 
     e2e_step()
     ems = timed(e2e_step, args.steps)
-    e_total = sum(ems)
-    if world > 1:
-        t = torch.tensor([e_total], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e_total = float(t.item())
-    e2e_value = world * args.steps * mpix / (e_total / 1e3)
+    e_total = max_over_ranks(sum(ems), dev)
+    e2e_value = job_throughput(world, args.steps, mpix, e_total)
 
     if rank != 0:
         if world > 1:
