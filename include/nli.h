@@ -283,6 +283,26 @@ int nli_update(nli_ctx *ctx, const nli_update_params *upd,
                const int32_t *nnf, const float *confidence, int W, int H, int C,
                double *total_difference);
 
+/* ---- adjoint of the image update ----------------------------------------- */
+/* Backward of one update step with the NNF held fixed (no reference
+ * counterpart: the reference is not differentiable).  The step is
+ * out = U(image; lambda, sigma) as nli_update computes it with orig = image
+ * (AImageUpdating::update, a_image_updating.h:34-39, as called by
+ * image_inpainting.cpp:394).  Given out (the forward result) and grad_out =
+ * dL/dout (W*H*C), writes grad_image = dL/dimage (W*H*C), *grad_lambda =
+ * dL/dlambda (the channels using upd->lambda), *grad_lambda_d = dL/dlambda_d
+ * (channel 3 of NLI_UPDATE_DEPTH, else 0) and *grad_sigma = dL/dsigma of the
+ * Gaussian patch weights.  NL-means: backward of the weighted average.
+ * NL-Poisson / NL-depth: a second CG solve A z = grad_out on the hole with
+ * the forward's system (upd->cg_tol, upd->cg_iters), then the adjoints of
+ * the coefficient gathers with the weights recomputed.  NL-medians returns
+ * NLI_E_UNSUPPORTED (piecewise constant).  Device pointers; blocks until the
+ * scalars are on the host. */
+int nli_update_backward(nli_ctx *ctx, const nli_update_params *upd, const float *image, const float *out,
+                        const uint8_t *domain, const uint8_t *ext_domain, const int32_t *nnf,
+                        const float *confidence, int W, int H, int C, const float *grad_out,
+                        float *grad_image, double *grad_lambda, double *grad_lambda_d, double *grad_sigma);
+
 /* ---- multiscale driver (L4) ---------------------------------------------- */
 /* ImageInpainting::process (image_inpainting.cpp:68-190).  Host pointers:
  * image (W*H*C floats), mask (W*H bytes), out (W*H*C floats).  The host

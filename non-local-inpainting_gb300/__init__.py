@@ -87,6 +87,8 @@ def load(path=LIB_PATH):
     proto("nli_bruteforce_nnf", I, [P, dp, P, P, I, I, P, P, I, I, I, P, P])
     proto("nli_patchmatch", I, [P, dp, pp, P, P, I, I, P, P, I, I, I, P, P, P, ct.POINTER(ct.c_double)])
     proto("nli_update", I, [P, up, P, P, P, P, P, P, I, I, I, ct.POINTER(ct.c_double)])
+    proto("nli_update_backward", I, [P, up, P, P, P, P, P, P, I, I, I, P, P, ct.POINTER(ct.c_double),
+                                     ct.POINTER(ct.c_double), ct.POINTER(ct.c_double)])
     proto("nli_process", I, [P, prp, P, P, I, I, I, P, st])
     proto("nli_process_device", I, [P, prp, P, P, I, I, I, P, st])
     proto("nli_process_batch", I, [P, I, prp, P, P, P, P, P, P, st, P])
@@ -318,6 +320,20 @@ class Context:
         self._check(self.lib.nli_update(self.h, ct.byref(upd), _ptr(img), _ptr(org), _ptr(dom), _ptr(ext), _ptr(nnf),
                                         _ptr(conf), W, H, C, ct.byref(tot)))
         return img, tot.value
+
+    def update_backward(self, upd, image, out, dom, ext, nnf, conf, grad_out):
+        """Adjoint of update(upd, image, image, ...) with the NNF fixed:
+        returns (dL/dimage, dL/dlambda, dL/dlambda_d, dL/dsigma)."""
+        img, out, g = self._f32(image), self._f32(out), self._f32(grad_out)
+        W, H, C = _dims(img)
+        dom, ext, nnf = self._u8(dom), self._u8(ext), self._i32(nnf)
+        conf = None if conf is None else self._f32(conf)
+        gi = self.torch.empty_like(img)
+        dl, dld, ds = ct.c_double(), ct.c_double(), ct.c_double()
+        self._check(self.lib.nli_update_backward(self.h, ct.byref(upd), _ptr(img), _ptr(out), _ptr(dom), _ptr(ext),
+                                                 _ptr(nnf), _ptr(conf), W, H, C, _ptr(g), _ptr(gi), ct.byref(dl),
+                                                 ct.byref(dld), ct.byref(ds)))
+        return gi, dl.value, dld.value, ds.value
 
     # -- L4
     def process(self, img, mask, params, stats=True):

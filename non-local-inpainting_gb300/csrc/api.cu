@@ -397,6 +397,20 @@ int nli_process(nli_ctx *ctx, const nli_process_params *params, const float *ima
 	API_END(ctx)
 }
 
+int nli_update_backward(nli_ctx *ctx, const nli_update_params *upd, const float *image, const float *out,
+                        const uint8_t *domain, const uint8_t *ext_domain, const int32_t *nnf,
+                        const float *confidence, int W, int H, int C, const float *grad_out, float *grad_image,
+                        double *grad_lambda, double *grad_lambda_d, double *grad_sigma)
+{
+	API_BEGIN(ctx)
+	require_ptrs({upd, image, out, domain, ext_domain, nnf, grad_out, grad_image, grad_lambda, grad_lambda_d,
+	              grad_sigma});
+	require_dims(W, H, C);
+	update_backward_run(ctx, *upd, image, out, domain, ext_domain, nnf, confidence, W, H, C, grad_out, grad_image,
+	                    grad_lambda, grad_lambda_d, grad_sigma);
+	API_END(ctx)
+}
+
 static void require_batch(int n, const void *params, const void *images, const void *masks, const void *widths,
                           const void *heights, const void *channels, const void *outputs)
 {

@@ -216,6 +216,12 @@ double update_run(nli_ctx *ctx, const nli_update_params &up, float *image, const
                   int H, int C, const int32_t *hole_list = nullptr, int n_hole = -1,
                   bool read_back = true);
 
+// Adjoint of one update with the NNF fixed (update.cu).
+void update_backward_run(nli_ctx *ctx, const nli_update_params &up, const float *image, const float *out,
+                         const uint8_t *dom, const uint8_t *ext, const int32_t *nnf, const float *conf, int W,
+                         int H, int C, const float *grad_out, float *grad_image, double *grad_lambda,
+                         double *grad_lambda_d, double *grad_sigma);
+
 // pyramid.cu
 void downsample_with_mask_run(nli_ctx *ctx, const float *img, const uint8_t *mask, int W, int H, int C,
                               float factor, float threshold, int mask_val, float *out_img,

@@ -833,28 +833,45 @@ static double read_total(nli_ctx *ctx, double *partials, int n, int *cg_iters_de
 	return *reinterpret_cast<double *>(h);
 }
 
-static void poisson_run(nli_ctx *ctx, const UpdArgs &u, const nli_update_params &up, float *image, const float *orig,
-                        const uint8_t *dom, const uint8_t *ext, const int2 *nnf, const float *conf,
-                        const int32_t *hole, const int32_t *hole_index, int nh, double *partials_out,
-                        int *n_partials)
+static void (*cluster_kernel(int CC))(PoissonArgs, int, const UnkC *, const float *, const float *, int *,
+                                      const int32_t *, const float *, float *, double *)
+{
+	return (CC == 1) ? k_poisson_cg_cluster<1>
+	       : (CC == 2) ? k_poisson_cg_cluster<2> : (CC == 3) ? k_poisson_cg_cluster<3> : k_poisson_cg_cluster<4>;
+}
+
+// Coefficients (gather), the compact system and its right-hand side b and
+// start x0 = image - orig (patch_non_local_poisson.cpp:36-82).  Chooses the
+// solver layout: `chunk` / `ncta` > 0 for the cluster CG.
+struct PoissonSystem {
+	PoissonArgs pa;
+	CoefOut co;
+	Unknown *unk;
+	float *b, *x;
+	int chunk = 0, ncta = 0;
+};
+
+static PoissonSystem poisson_system(nli_ctx *ctx, const UpdArgs &u, const nli_update_params &up, const float *image,
+                                    const float *orig, const uint8_t *dom, const uint8_t *ext, const int2 *nnf,
+                                    const float *conf, const int32_t *hole, const int32_t *hole_index, int nh)
 {
 	cudaStream_t s = ctx->stream;
 	const int W = u.W, H = u.H, C = u.C;
 	const size_t n = (size_t)W * H;
+	PoissonSystem P;
 	float *grad = ctx->buf<float>("poi.grad", n * 2 * C);
 	launch_gradient(s, image, W, H, C, grad);
-	CoefOut co;
-	co.S = ctx->buf<float>("poi.S", n);
-	co.U = ctx->buf<float>("poi.U", n * C);
-	co.GX = ctx->buf<float>("poi.GX", n * C);
-	co.GY = ctx->buf<float>("poi.GY", n * C);
+	P.co.S = ctx->buf<float>("poi.S", n);
+	P.co.U = ctx->buf<float>("poi.U", n * C);
+	P.co.GX = ctx->buf<float>("poi.GX", n * C);
+	P.co.GY = ctx->buf<float>("poi.GY", n * C);
 	{
-	ProfScope ps(ctx, "poisson_coef");
-	k_poisson_coef<<<(nh + 127) / 128, 128, 0, s>>>(u, hole, nh, dom, ext, nnf, conf, image,
-	                                                 reinterpret_cast<const float2 *>(grad), co);
-	NLI_CHECK_LAUNCH();
+		ProfScope ps(ctx, "poisson_coef");
+		k_poisson_coef<<<(nh + 127) / 128, 128, 0, s>>>(u, hole, nh, dom, ext, nnf, conf, image,
+		                                                 reinterpret_cast<const float2 *>(grad), P.co);
+		NLI_CHECK_LAUNCH();
 	}
-	PoissonArgs pa;
+	PoissonArgs &pa = P.pa;
 	pa.W = W;
 	pa.H = H;
 	pa.C = C;
@@ -863,18 +880,11 @@ static void poisson_run(nli_ctx *ctx, const UpdArgs &u, const nli_update_params 
 	if (up.method == NLI_UPDATE_DEPTH) pa.lambda[3] = up.lambda_d;
 	pa.tol = up.cg_tol;
 	pa.limit = up.cg_iters;
-	Unknown *unk = ctx->buf<Unknown>("poi.unk", nh);
-	float *b = ctx->buf<float>("poi.b", (size_t)nh * C);
-	float *x = ctx->buf<float>("poi.x", (size_t)nh * C);
-	float *r = ctx->buf<float>("poi.r", (size_t)nh * C);
-	float *d = ctx->buf<float>("poi.d", (size_t)nh * C);
-	float *q = ctx->buf<float>("poi.q", (size_t)nh * C);
-	// shared-memory cluster kernel: kClusterVectors vectors x C channels x chunk floats per CTA
+	P.unk = ctx->buf<Unknown>("poi.unk", nh);
+	P.b = ctx->buf<float>("poi.b", (size_t)nh * C);
+	P.x = ctx->buf<float>("poi.x", (size_t)nh * C);
+	// shared-memory cluster kernel: kClusterVectors vectors x chunk floats per CTA, one cluster per channel
 	constexpr size_t kSmemBudget = 216 * 1024;
-	auto cluster_kernel = [](int CC) {
-		return (CC == 1) ? k_poisson_cg_cluster<1>
-		       : (CC == 2) ? k_poisson_cg_cluster<2> : (CC == 3) ? k_poisson_cg_cluster<3> : k_poisson_cg_cluster<4>;
-	};
 	if (ctx->cg_cluster_max < 0) {
 		// largest cluster the device runs with the biggest shared-memory footprint
 		int maxc = 0;
@@ -894,51 +904,54 @@ static void poisson_run(nli_ctx *ctx, const UpdArgs &u, const nli_update_params 
 		cudaGetLastError();
 		ctx->cg_cluster_max = std::min(maxc, kClusterMax);
 	}
-	int ncta = 0, chunk = 0;
 	if (ctx->cg_cluster_max >= 1) {
-		ncta = std::max(1, std::min(ctx->cg_cluster_max, (nh + 2 * kClusterBlock - 1) / (2 * kClusterBlock)));
-		chunk = (nh + ncta - 1) / ncta;
-		if ((size_t)kClusterVectors * chunk * sizeof(float) + chunk * sizeof(UnkC) > kSmemBudget ||
-		    chunk > kClusterMaxChunk)
-			ncta = chunk = 0;
+		P.ncta = std::max(1, std::min(ctx->cg_cluster_max, (nh + 2 * kClusterBlock - 1) / (2 * kClusterBlock)));
+		P.chunk = (nh + P.ncta - 1) / P.ncta;
+		if ((size_t)kClusterVectors * P.chunk * sizeof(float) + P.chunk * sizeof(UnkC) > kSmemBudget ||
+		    P.chunk > kClusterMaxChunk)
+			P.ncta = P.chunk = 0;
 	}
 	{
 		ProfScope ps(ctx, "poisson_setup");
-		k_poisson_setup<<<(nh + 255) / 256, 256, 0, s>>>(pa, chunk, hole, hole_index, co, image, orig, unk, b, x);
+		k_poisson_setup<<<(nh + 255) / 256, 256, 0, s>>>(pa, P.chunk, hole, hole_index, P.co, image, orig, P.unk,
+		                                                  P.b, P.x);
 		NLI_CHECK_LAUNCH();
 	}
+	return P;
+}
 
+// Solves the system from x0 (the CG of :387-477) and writes u = orig + x on
+// the hole into img, with per-block partial sums of (u_old - u_new)^2 in
+// "poi.diff" (returns their count).
+static int poisson_solve(nli_ctx *ctx, PoissonSystem &P, const int32_t *hole, const float *orig, float *img)
+{
+	cudaStream_t s = ctx->stream;
+	const int nh = P.pa.nh, C = P.pa.C;
 	int *iters = ctx->buf<int>("poi.iters", 4);
-	const float *orig_c = orig;
-	if (ncta > 0) {
-		// one cluster per channel
-		const size_t smem = (size_t)kClusterVectors * chunk * sizeof(float) + chunk * sizeof(UnkC);
+	if (P.ncta > 0) {
+		const size_t smem = (size_t)kClusterVectors * P.chunk * sizeof(float) + P.chunk * sizeof(UnkC);
 		UnkC *unkc = ctx->buf<UnkC>("poi.unkc", nh);
-		k_poisson_compact<<<(nh + 255) / 256, 256, 0, s>>>(unk, nh, chunk, unkc);
+		k_poisson_compact<<<(nh + 255) / 256, 256, 0, s>>>(P.unk, nh, P.chunk, unkc);
 		NLI_CHECK_LAUNCH();
-		{
-			double *diff_part = ctx->buf<double>("poi.diff", (size_t)C * ncta + 1);
-			cudaLaunchConfig_t cfg = {};
-			cfg.gridDim = dim3(C * ncta);
-			cfg.blockDim = dim3(kClusterBlock);
-			cfg.dynamicSmemBytes = smem;
-			cfg.stream = s;
-			cudaLaunchAttribute attr[1];
-			attr[0].id = cudaLaunchAttributeClusterDimension;
-			attr[0].val.clusterDim.x = ncta;
-			attr[0].val.clusterDim.y = 1;
-			attr[0].val.clusterDim.z = 1;
-			cfg.attrs = attr;
-			cfg.numAttrs = 1;
-			ProfScope ps(ctx, "poisson_cg");
-			NLI_CUDA(cudaLaunchKernelEx(&cfg, cluster_kernel(1), pa, chunk, (const UnkC *)unkc, (const float *)b,
-			                            (const float *)x, iters, hole, orig_c, image, diff_part));
-			nli_count_launch_internal();
-			*n_partials = C * ncta;
-			return;
-		}
+		double *diff_part = ctx->buf<double>("poi.diff", (size_t)C * P.ncta + 1);
+		cudaLaunchConfig_t cfg = {};
+		cfg.gridDim = dim3(C * P.ncta);
+		cfg.blockDim = dim3(kClusterBlock);
+		cfg.dynamicSmemBytes = smem;
+		cfg.stream = s;
+		cudaLaunchAttribute attr[1];
+		attr[0].id = cudaLaunchAttributeClusterDimension;
+		attr[0].val.clusterDim.x = P.ncta;
+		attr[0].val.clusterDim.y = 1;
+		attr[0].val.clusterDim.z = 1;
+		cfg.attrs = attr;
+		cfg.numAttrs = 1;
+		ProfScope ps(ctx, "poisson_cg");
+		NLI_CUDA(cudaLaunchKernelEx(&cfg, cluster_kernel(1), P.pa, P.chunk, (const UnkC *)unkc, (const float *)P.b,
+		                            (const float *)P.x, iters, hole, orig, img, diff_part));
+		nli_count_launch_internal();
+		return C * P.ncta;
 	}
-
 	int dev_blocks_per_sm = 0;
 	NLI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&dev_blocks_per_sm, k_poisson_cg, kCgBlock, 0));
 	const int max_blocks = dev_blocks_per_sm * ctx->num_sms;
@@ -947,16 +960,29 @@ static void poisson_run(nli_ctx *ctx, const UpdArgs &u, const nli_update_params 
 	grid = std::min(std::max(grid, 1), std::min(max_blocks, ctx->num_sms));
 	double *part = ctx->buf<double>("poi.part", (size_t)grid * 8);
 	double *diff_part = ctx->buf<double>("poi.diff", grid + 1);
+	float *r = ctx->buf<float>("poi.r", (size_t)nh * C);
+	float *d = ctx->buf<float>("poi.d", (size_t)nh * C);
+	float *q = ctx->buf<float>("poi.q", (size_t)nh * C);
 	NLI_CUDA(cudaMemsetAsync(ctx->status, 0, sizeof(DevStatus), s));
 	DevStatus *st = ctx->status;
-	void *args[] = {&pa, &unk, &b, &x, &r, &d, &q, &part, &st, &iters, (void *)&hole, &orig_c, &image, &diff_part};
+	const Unknown *unk = P.unk;
+	const float *b = P.b;
+	float *x = P.x;
+	void *args[] = {&P.pa, &unk, &b, &x, &r, &d, &q, &part, &st, &iters, (void *)&hole, &orig, &img, &diff_part};
 	{
 		ProfScope ps(ctx, "poisson_cg");
 		NLI_CUDA(cudaLaunchCooperativeKernel((const void *)k_poisson_cg, dim3(grid), dim3(kCgBlock), args, 0, s));
 		nli_count_launch_internal();
 	}
-	*n_partials = grid;
-	(void)partials_out;
+	return grid;
+}
+
+static void poisson_run(nli_ctx *ctx, const UpdArgs &u, const nli_update_params &up, float *image, const float *orig,
+                        const uint8_t *dom, const uint8_t *ext, const int2 *nnf, const float *conf,
+                        const int32_t *hole, const int32_t *hole_index, int nh, int *n_partials)
+{
+	PoissonSystem P = poisson_system(ctx, u, up, image, orig, dom, ext, nnf, conf, hole, hole_index, nh);
+	*n_partials = poisson_solve(ctx, P, hole, orig, image);
 }
 
 double update_run(nli_ctx *ctx, const nli_update_params &up, float *image, const float *orig, const uint8_t *dom,
@@ -984,7 +1010,7 @@ double update_run(nli_ctx *ctx, const nli_update_params &up, float *image, const
 		NLI_CHECK_LAUNCH();
 		hole_index = idx;
 		int np = 0;
-		poisson_run(ctx, u, up, image, orig, dom, ext, nnf, conf, hole, hole_index, nh, nullptr, &np);
+		poisson_run(ctx, u, up, image, orig, dom, ext, nnf, conf, hole, hole_index, nh, &np);
 		double *diff_part = ctx->buf<double>("poi.diff", np + 1);
 		if (!read_back) {
 			launch_sum_partials(s, diff_part, np, diff_part + np);
@@ -1018,6 +1044,361 @@ double update_run(nli_ctx *ctx, const nli_update_params &up, float *image, const
 		return 0.0;
 	}
 	return read_total(ctx, partials, grid, nullptr, C);
+}
+
+// ============================================================== adjoints
+// Backward of one image update with the NNF held fixed: out = U(u; lambda,
+// sigma) with orig = u (the update step of image_inpainting.cpp:394 on its
+// own), given g = dL/dout.  The NNF is an integer argmin and is not
+// differentiated.  Accumulation into dL/du is in double (atomics), then
+// rounded to float.  sigma enters through the normalised Gaussian patch
+// weights w_k = e_k / sum_j e_j, e_k = exp(-r_k^2 / (2 sigma^2))
+// (gaussian_weights.cpp:19-79): dw_k/dsigma = w_k (rho_k - m), rho_k =
+// r_k^2 / sigma^3, m = sum_j w_j rho_j.
+struct AdjArgs {
+	double sigma3;  // sigma^3
+	double m;       // sum_j w_j rho_j of the weight table
+};
+
+__device__ __forceinline__ double tap_rho(const UpdArgs &u, const AdjArgs &a, int k)
+{
+	const int kx = k % u.px - u.hx, ky = k / u.px - u.hy;
+	return (double)(kx * kx + ky * ky) / a.sigma3;
+}
+
+// Identity part: out = u outside the domain (and on domain pixels without
+// any valid candidate, handled by the means kernel).
+__global__ void k_adj_init(const float *__restrict__ g, const uint8_t *__restrict__ dom, int n, int C,
+                           double *__restrict__ gacc)
+{
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n * C; i += gridDim.x * blockDim.x)
+		gacc[i] = dom[i / C] ? 0.0 : (double)g[i];
+}
+
+// NL-means: out_c(p) = N_c / D, N_c = sum_i w_i u_c(s_i), D = sum_i w_i, with
+// the forward's weights (clipped-corner table index, confidence inside the
+// domain).  du(s_i) += g_c w_i / D; dsigma += sum_c g_c sum_i w_i rho_i
+// (u_c(s_i) - out_c) / D (the normalisation term cancels in the ratio).
+__global__ void __launch_bounds__(256) k_means_backward(UpdArgs u, AdjArgs a, const float *__restrict__ img,
+                                                        const int32_t *__restrict__ hole, int nh,
+                                                        const uint8_t *__restrict__ dom, const int2 *__restrict__ nnf,
+                                                        const float *__restrict__ conf, const float *__restrict__ g,
+                                                        double *__restrict__ gacc, double *__restrict__ partials)
+{
+	__shared__ double red[8];
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	double dsig = 0.0;
+	if (i < nh) {
+		const int W = u.W, H = u.H, C = u.C;
+		const int pix = hole[i];
+		const int x = pix % W, y = pix / W;
+		const int x_a = max(x - u.hx, 0), x_b = min(x + u.hx, W - 1);
+		const int y_a = max(y - u.hy, 0), y_b = min(y + u.hy, H - 1);
+		float tv[4] = {0.f, 0.f, 0.f, 0.f};
+		float tw = 0.f;
+		for (int ii = x_a; ii <= x_b; ii++)
+			for (int jj = y_a; jj <= y_b; jj++) {
+				int2 q = nnf[jj * W + ii];
+				if (q.x == -1) continue;
+				q.x += x - ii;
+				q.y += y - jj;
+				if (q.x < 0 || q.y < 0 || q.x >= W || q.y >= H) continue;
+				float w = u.weights[(jj - y_a) * u.px + (ii - x_a)];
+				if (conf && dom[jj * W + ii]) w = fm(w, conf[jj * W + ii]);
+				tw = fa(tw, w);
+				const float *sv = img + (size_t)C * (q.y * W + q.x);
+				for (int c = 0; c < C; c++) tv[c] = fa(tv[c], fm(sv[c], w));
+			}
+		const float *gp = g + (size_t)C * pix;
+		if (tw > 0.0f) {
+			float out[4];
+			for (int c = 0; c < C; c++) out[c] = __fdiv_rn(tv[c], tw);
+			const double inv = 1.0 / (double)tw;
+			for (int ii = x_a; ii <= x_b; ii++)
+				for (int jj = y_a; jj <= y_b; jj++) {
+					int2 q = nnf[jj * W + ii];
+					if (q.x == -1) continue;
+					q.x += x - ii;
+					q.y += y - jj;
+					if (q.x < 0 || q.y < 0 || q.x >= W || q.y >= H) continue;
+					const int k = (jj - y_a) * u.px + (ii - x_a);
+					float w = u.weights[k];
+					if (conf && dom[jj * W + ii]) w = fm(w, conf[jj * W + ii]);
+					const double wd = (double)w * inv, rho = tap_rho(u, a, k);
+					const size_t s = (size_t)C * (q.y * W + q.x);
+					for (int c = 0; c < C; c++) {
+						atomicAdd(gacc + s + c, (double)gp[c] * wd);
+						dsig += (double)gp[c] * wd * rho * ((double)img[s + c] - (double)out[c]);
+					}
+				}
+		} else {
+			for (int c = 0; c < C; c++) atomicAdd(gacc + (size_t)C * pix + c, (double)gp[c]);
+		}
+	}
+	dsig = block_sum<256>(dsig, red);
+	if (threadIdx.x == 0) partials[blockIdx.x] = dsig;
+}
+
+// NL-Poisson, per pixel q: the adjoints of the coefficients S(q), U(q),
+// GX(q), GY(q) for the residual F_k = lambda U_k - (1-lambda) D_k -
+// lambda S_k out_k + (1-lambda) sum_nb s_nb(k) (out_nb - out_k) (D = the
+// backward divergence of (GX, GY), s_up / s_left = S of that neighbour,
+// s_down / s_right = S_k), weighted by the adjoint solution z = A^-1 g on
+// the hole; the identity and boundary-coupling part of dL/du for pixels
+// outside the hole; and dL/dlambda per hole pixel.
+struct AdjCoef {
+	float *dS;   // W*H
+	float *dU;   // W*H*C
+	float *dGX;  // W*H*C
+	float *dGY;  // W*H*C
+	uint8_t *active;
+};
+
+__global__ void k_poisson_adj_coef(PoissonArgs pa, CoefOut co, AdjCoef ad, const uint8_t *__restrict__ dom,
+                                   const float *__restrict__ out, const float *__restrict__ z,
+                                   const float *__restrict__ g, double *__restrict__ gacc,
+                                   double *__restrict__ lam_part, int depth)
+{
+	__shared__ double red[2][8];
+	const int W = pa.W, H = pa.H, C = pa.C;
+	const int q = blockIdx.x * blockDim.x + threadIdx.x;
+	double dl = 0.0, dld = 0.0;
+	if (q < W * H) {
+		const int x = q % W, y = q / W;
+		const bool hq = dom[q] != 0;
+		const bool hr = (x != W - 1) && dom[q + 1];
+		const bool hd = (y != H - 1) && dom[q + W];
+		const bool hl = (x != 0) && dom[q - 1];
+		const bool hu = (y != 0) && dom[q - W];
+		const bool act = hq || hr || hd;
+		ad.active[q] = act ? 1 : 0;
+		float dS = 0.f;
+		for (int c = 0; c < C; c++) {
+			const float lam = pa.lambda[c], oml = 1.0f - lam;
+			const size_t o = (size_t)C * q + c;
+			const float zq = hq ? z[o] : 0.f;
+			const float zr = hr ? z[o + C] : 0.f;
+			const float zd = hd ? z[o + (size_t)C * W] : 0.f;
+			const float oq = out[o];
+			if (act) {
+				ad.dU[o] = lam * zq;
+				ad.dGX[o] = (x != W - 1) ? oml * (zr - zq) : 0.f;
+				ad.dGY[o] = (y != H - 1) ? oml * (zd - zq) : 0.f;
+				float s = 0.f;
+				if (hq) {
+					s -= lam * oq;
+					if (y != H - 1) s += oml * (out[o + (size_t)C * W] - oq);
+					if (x != W - 1) s += oml * (out[o + C] - oq);
+					s *= zq;
+				}
+				if (hd) s += zd * oml * (oq - out[o + (size_t)C * W]);
+				if (hr) s += zr * oml * (oq - out[o + C]);
+				dS += s;
+			}
+			if (hq) {
+				// dF_k / dlambda
+				const float Sk = co.S[q];
+				float Dk = 0.f;
+				if (x != W - 1) Dk += co.GX[o];
+				if (x != 0) Dk -= co.GX[o - C];
+				if (y != H - 1) Dk += co.GY[o];
+				if (y != 0) Dk -= co.GY[o - (size_t)C * W];
+				float lap = 0.f;
+				if (y != 0) lap += co.S[q - W] * (out[o - (size_t)C * W] - oq);
+				if (x != 0) lap += co.S[q - 1] * (out[o - C] - oq);
+				if (y != H - 1) lap += Sk * (out[o + (size_t)C * W] - oq);
+				if (x != W - 1) lap += Sk * (out[o + C] - oq);
+				const double v = (double)zq * ((double)co.U[o] + Dk - (double)Sk * oq - lap);
+				if (depth && c == 3)
+					dld += v;
+				else
+					dl += v;
+			} else {
+				// identity and the coupling into the hole's stencil:
+				// (1 - lambda) sum over hole neighbours k of z_k s_q(k)
+				double v = (double)g[o];
+				if (hd) v += (double)oml * z[o + (size_t)C * W] * co.S[q];       // q is the upper neighbour of k
+				if (hu) v += (double)oml * z[o - (size_t)C * W] * co.S[q - W];   // q is the lower neighbour
+				if (hr) v += (double)oml * z[o + C] * co.S[q];                   // q is the left neighbour
+				if (hl) v += (double)oml * z[o - C] * co.S[q - 1];               // q is the right neighbour
+				atomicAdd(gacc + o, v);
+			}
+		}
+		if (act) ad.dS[q] = dS;
+	}
+	dl = block_sum<256>(dl, red[0]);
+	dld = block_sum<256>(dld, red[1]);
+	if (threadIdx.x == 0) {
+		lam_part[2 * blockIdx.x] = dl;
+		lam_part[2 * blockIdx.x + 1] = dld;
+	}
+}
+
+// Scatter of the coefficient adjoints through the gathers of
+// k_poisson_coef: for every active q and every extended-domain centre c of
+// its window with n = nnf(c) + q - c in the image,
+//   du(n) += w dU(q), gx / gy of n (forward differences of u) take w dGX(q),
+//   w dGY(q), and dsigma += dw/dsigma (dS(q) + sum_c dU u(n) + dGX gx(n) +
+//   dGY gy(n)).
+__global__ void __launch_bounds__(128) k_poisson_adj_scatter(UpdArgs u, AdjArgs a, AdjCoef ad,
+                                                             const uint8_t *__restrict__ ext,
+                                                             const int2 *__restrict__ nnf,
+                                                             const float *__restrict__ conf,
+                                                             const float *__restrict__ img,
+                                                             const float2 *__restrict__ grad,
+                                                             double *__restrict__ gacc, double *__restrict__ partials)
+{
+	__shared__ double red[4];
+	const int W = u.W, H = u.H, C = u.C;
+	const int q = blockIdx.x * blockDim.x + threadIdx.x;
+	double dsig = 0.0;
+	if (q < W * H && ad.active[q]) {
+		const int qx = q % W, qy = q / W;
+		float dU[4], dGX[4], dGY[4];
+		for (int c = 0; c < C; c++) {
+			dU[c] = ad.dU[(size_t)C * q + c];
+			dGX[c] = ad.dGX[(size_t)C * q + c];
+			dGY[c] = ad.dGY[(size_t)C * q + c];
+		}
+		const double dS = ad.dS[q];
+		const int cy0 = max(qy - u.hy, 0), cy1 = min(qy + u.hy, H - 1);
+		const int cx0 = max(qx - u.hx, 0), cx1 = min(qx + u.hx, W - 1);
+		for (int cy = cy0; cy <= cy1; cy++)
+			for (int cx = cx0; cx <= cx1; cx++) {
+				const int c0 = cy * W + cx;
+				if (!ext[c0]) continue;
+				const int2 nb = nnf[c0];
+				const int nx = nb.x + qx - cx, ny = nb.y + qy - cy;
+				if (nx < 0 || ny < 0 || nx >= W || ny >= H) continue;
+				const int k = (qy - cy + u.hy) * u.px + (qx - cx + u.hx);
+				const double cf = conf ? (double)conf[c0] : 1.0;
+				const double w = cf * (double)u.weights[k];
+				const double dw = w * (tap_rho(u, a, k) - a.m);
+				const int n = ny * W + nx;
+				double t = dS;
+				for (int c = 0; c < C; c++) {
+					const size_t o = (size_t)C * n + c;
+					const float2 gv = grad[o];
+					t += (double)dU[c] * img[o] + (double)dGX[c] * gv.x + (double)dGY[c] * gv.y;
+					double own = w * dU[c];
+					if (nx != W - 1) {
+						atomicAdd(gacc + o + C, w * dGX[c]);
+						own -= w * dGX[c];
+					}
+					if (ny != H - 1) {
+						atomicAdd(gacc + o + (size_t)C * W, w * dGY[c]);
+						own -= w * dGY[c];
+					}
+					atomicAdd(gacc + o, own);
+				}
+				dsig += dw * t;
+			}
+	}
+	dsig = block_sum<128>(dsig, red);
+	if (threadIdx.x == 0) partials[blockIdx.x] = dsig;
+}
+
+__global__ void k_hole_to_planar(const float *__restrict__ g, const int32_t *__restrict__ hole, int nh, int C,
+                                 float *__restrict__ b)
+{
+	const int i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= nh * C) return;
+	const int k = i % nh, c = i / nh;
+	b[i] = g[(size_t)C * hole[k] + c];
+}
+
+__global__ void k_to_float(const double *__restrict__ a, size_t n, float *__restrict__ out)
+{
+	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+		out[i] = (float)a[i];
+}
+
+static double sum_on_host(nli_ctx *ctx, const double *partials, int n, int stride, int offset)
+{
+	std::vector<double> h((size_t)n * stride);
+	NLI_CUDA(cudaMemcpyAsync(h.data(), partials, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, ctx->stream));
+	NLI_CUDA(cudaStreamSynchronize(ctx->stream));
+	double s = 0.0;
+	for (int i = 0; i < n; i++) s += h[(size_t)i * stride + offset];
+	return s;
+}
+
+void update_backward_run(nli_ctx *ctx, const nli_update_params &up, const float *image, const float *out,
+                         const uint8_t *dom, const uint8_t *ext, const int32_t *nnf_i, const float *conf, int W,
+                         int H, int C, const float *grad_out, float *grad_image, double *grad_lambda,
+                         double *grad_lambda_d, double *grad_sigma)
+{
+	NLI_REQUIRE(up.method == NLI_UPDATE_MEANS || up.method == NLI_UPDATE_POISSON || up.method == NLI_UPDATE_DEPTH,
+	            NLI_E_UNSUPPORTED, "no adjoint for this update method (the weighted median is piecewise constant)");
+	if (up.method == NLI_UPDATE_DEPTH) NLI_REQUIRE(C == 4, NLI_E_CHANNELS, "Separate: Channels do not match.");
+	UpdArgs u;
+	fill_upd_args(u, up, W, H, C);
+	AdjArgs a;
+	a.sigma3 = (double)up.sigma * up.sigma * up.sigma;
+	a.m = 0.0;
+	for (int k = 0; k < u.px * u.py; k++) {
+		const int kx = k % u.px - u.hx, ky = k / u.px - u.hy;
+		a.m += (double)u.weights[k] * (double)(kx * kx + ky * ky) / a.sigma3;
+	}
+	cudaStream_t s = ctx->stream;
+	const size_t n = (size_t)W * H;
+	const int2 *nnf = reinterpret_cast<const int2 *>(nnf_i);
+	int32_t *hole = ctx->buf<int32_t>("adj.hole", n);
+	const int nh = compact_mask(ctx, dom, W, H, hole, "adj");
+	double *gacc = ctx->buf<double>("adj.gacc", n * C);
+	k_adj_init<<<(int)std::min<size_t>((n * C + 255) / 256, 8192), 256, 0, s>>>(grad_out, dom, (int)n, C, gacc);
+	NLI_CHECK_LAUNCH();
+	*grad_lambda = 0.0;
+	*grad_lambda_d = 0.0;
+	*grad_sigma = 0.0;
+	if (nh > 0 && up.method == NLI_UPDATE_MEANS) {
+		const int grid = (nh + 255) / 256;
+		double *part = ctx->buf<double>("adj.part", grid);
+		k_means_backward<<<grid, 256, 0, s>>>(u, a, image, hole, nh, dom, nnf, conf, grad_out, gacc, part);
+		NLI_CHECK_LAUNCH();
+		*grad_sigma = sum_on_host(ctx, part, grid, 1, 0);
+	} else if (nh > 0) {
+		int32_t *idx = ctx->buf<int32_t>("upd.hole_index", n);
+		k_fill_int<<<(int)((n + 255) / 256), 256, 0, s>>>(idx, (int)n, -1);
+		NLI_CHECK_LAUNCH();
+		k_hole_index<<<(nh + 255) / 256, 256, 0, s>>>(hole, nh, idx);
+		NLI_CHECK_LAUNCH();
+		// system of the forward step with orig = image; its right-hand side
+		// is replaced by g on the hole, and z = A^-1 g is written as an image
+		PoissonSystem P = poisson_system(ctx, u, up, image, image, dom, ext, nnf, conf, hole, idx, nh);
+		k_hole_to_planar<<<(nh * C + 255) / 256, 256, 0, s>>>(grad_out, hole, nh, C, P.b);
+		NLI_CHECK_LAUNCH();
+		NLI_CUDA(cudaMemsetAsync(P.x, 0, sizeof(float) * nh * C, s));
+		float *zimg = ctx->buf<float>("adj.z", n * C);
+		float *zero = ctx->buf<float>("adj.zero", n * C);
+		NLI_CUDA(cudaMemsetAsync(zimg, 0, sizeof(float) * n * C, s));
+		NLI_CUDA(cudaMemsetAsync(zero, 0, sizeof(float) * n * C, s));
+		const int np = poisson_solve(ctx, P, hole, zero, zimg);
+		(void)read_total(ctx, ctx->buf<double>("poi.diff", np + 1), np, ctx->buf<int>("poi.iters", 4), C, nh);
+		AdjCoef ad;
+		ad.dS = ctx->buf<float>("adj.dS", n);
+		ad.dU = ctx->buf<float>("adj.dU", n * C);
+		ad.dGX = ctx->buf<float>("adj.dGX", n * C);
+		ad.dGY = ctx->buf<float>("adj.dGY", n * C);
+		ad.active = ctx->buf<uint8_t>("adj.active", n);
+		const int grid = (int)((n + 255) / 256);
+		double *lam_part = ctx->buf<double>("adj.lam", 2 * (size_t)grid);
+		k_poisson_adj_coef<<<grid, 256, 0, s>>>(P.pa, P.co, ad, dom, out, zimg, grad_out, gacc, lam_part,
+		                                        up.method == NLI_UPDATE_DEPTH ? 1 : 0);
+		NLI_CHECK_LAUNCH();
+		const int grid2 = (int)((n + 127) / 128);
+		double *sig_part = ctx->buf<double>("adj.sig", grid2);
+		k_poisson_adj_scatter<<<grid2, 128, 0, s>>>(u, a, ad, ext, nnf, conf, image,
+		                                            reinterpret_cast<const float2 *>(ctx->buf<float>("poi.grad", n * 2 * C)),
+		                                            gacc, sig_part);
+		NLI_CHECK_LAUNCH();
+		*grad_lambda = sum_on_host(ctx, lam_part, grid, 2, 0);
+		*grad_lambda_d = sum_on_host(ctx, lam_part, grid, 2, 1);
+		*grad_sigma = sum_on_host(ctx, sig_part, grid2, 1, 0);
+	}
+	k_to_float<<<(int)std::min<size_t>((n * C + 255) / 256, 8192), 256, 0, s>>>(gacc, n * C, grad_image);
+	NLI_CHECK_LAUNCH();
+	NLI_CUDA(cudaStreamSynchronize(s));
 }
 
 }  // namespace nli

@@ -1,0 +1,143 @@
+"""Adjoint kernels of the image update (NNF held fixed): gradients with
+respect to the image, lambda and the patch-weight sigma, from the CUDA
+backward (through the torch.autograd.Function), against an FP64 PyTorch
+re-expression of the same step (tests/update64.py): its autograd gradients
+at small sizes and FP64 central finite differences (step 1e-3) along random
+directions.  Tolerance: 1e-4 relative."""
+import numpy as np
+import pytest
+import torch
+
+import update64
+
+pytestmark = pytest.mark.gpu
+
+
+def make_case(ctx, size, seed, method, sigma=10000.0, lam=0.05):
+    from nli_gb300 import workloads as wl
+    img, mask, _ = wl.config2(seed=seed, size=size, scales=3)
+    p = wl.params(method, scales=3, coarse=0.5, iters=10, cg_tol=1e-12, cg_iters=1000, psigma=sigma, lam=lam)
+    ext = ctx.extended_domain(mask, 9, 9)
+    src, tgt, _ = ctx.scale_masks(ext, 4, True)
+    u = ctx.poisson_init(img, mask)  # hole filled smoothly, as the coarsest level starts
+    ctx.set_seed(seed)
+    nnf, _, _ = ctx.patchmatch(p.distance, p.patchmatch, u, src, u, tgt)
+    conf = ctx.confidence_mask(mask, 5.0, 0.1)
+    rng = np.random.default_rng(seed + 1)
+    target = torch.from_numpy(rng.uniform(0, 255, img.shape).astype(np.float32)).cuda()
+    return dict(p=p, u=u, mask=mask, ext=ext, nnf=nnf, conf=conf, target=target, hole=torch.from_numpy(mask != 0).cuda())
+
+
+def ours(ctx, case, lam, sigma):
+    from nli_gb300.autograd import image_update
+    u = case["u"].detach().clone().requires_grad_(True)
+    lt = torch.tensor(lam, dtype=torch.float64, requires_grad=True)
+    st = torch.tensor(sigma, dtype=torch.float64, requires_grad=True)
+    out = image_update(ctx, case["p"].update, u, lt, st, case["mask"], case["ext"], case["nnf"], case["conf"])
+    loss = (((out - case["target"]) ** 2) * case["hole"][..., None]).sum()
+    loss.backward()
+    return out.detach(), u.grad.double().cpu(), float(lt.grad), float(st.grad)
+
+
+def ref64(case, method, lam, sigma, u=None, solver="dense"):
+    """(loss, out) of the FP64 re-expression; u defaults to the case image."""
+    u = case["u"].double().cpu() if u is None else u
+    nnf = case["nnf"].cpu().numpy().reshape(u.shape[0], u.shape[1], 2)
+    dom = case["mask"] != 0
+    ext = case["ext"].cpu().numpy() if torch.is_tensor(case["ext"]) else case["ext"]
+    conf = case["conf"].double().cpu().numpy()
+    if method == "nlmeans":
+        out = update64.means(u, sigma, nnf, dom, conf)
+    else:
+        out = update64.poisson(u, lam, sigma, nnf, dom, ext, conf, solver=solver)
+    t = case["target"].double().cpu()
+    loss = (((out - t) ** 2) * torch.from_numpy(dom)[..., None]).sum()
+    return loss, out
+
+
+def rel(a, b):
+    return float(torch.linalg.norm(a - b) / max(float(torch.linalg.norm(b)), 1e-300))
+
+
+@pytest.mark.parametrize("method,sigma", [("nlmeans", 10000.0), ("nlmeans", 3.0), ("nlpoisson", 10000.0),
+                                          ("nlpoisson", 3.0)])
+def test_gradients_match_fp64_autograd(gpu_ctx, method, sigma):
+    case = make_case(gpu_ctx, 64, 21, method, sigma=sigma)
+    lam = 0.05
+    out, gu, gl, gs = ours(gpu_ctx, case, lam, sigma)
+    u64 = case["u"].double().cpu().requires_grad_(True)
+    l64 = torch.tensor(lam, dtype=torch.float64, requires_grad=True)
+    s64 = torch.tensor(sigma, dtype=torch.float64, requires_grad=True)
+    loss, out64 = ref64(case, method, l64, s64, u=u64)
+    loss.backward()
+    print("64x64 %s sigma %g: out %.3g, d/du %.3g, d/dlambda %.3g, d/dsigma %.3g (relative to FP64)" % (
+        method, sigma, rel(out.double().cpu(), out64.detach()), rel(gu, u64.grad),
+        abs(gl - float(l64.grad)) / abs(float(l64.grad)) if l64.grad is not None else 0.0,
+        abs(gs - float(s64.grad)) / abs(float(s64.grad))))
+    assert rel(out.double().cpu(), out64.detach()) < 1e-5
+    assert rel(gu, u64.grad) < 1e-4, rel(gu, u64.grad)
+    if method == "nlmeans":
+        assert gl == 0.0  # NL-means does not depend on lambda
+    else:
+        assert abs(gl - float(l64.grad)) <= 1e-4 * abs(float(l64.grad)), (gl, float(l64.grad))
+    assert abs(gs - float(s64.grad)) <= 1e-4 * abs(float(s64.grad)) + 1e-12, (gs, float(s64.grad))
+
+
+@pytest.mark.parametrize("method", ["nlmeans", "nlpoisson"])
+def test_directional_finite_differences(gpu_ctx, method):
+    """64 random directions over (known pixels, lambda, sigma); central
+    differences of the FP64 loss with step 1e-3."""
+    sigma, lam = 3.0, 0.05
+    case = make_case(gpu_ctx, 48, 22, method, sigma=sigma)
+    _, gu, gl, gs = ours(gpu_ctx, case, lam, sigma)
+    known = torch.from_numpy(case["mask"] == 0)[..., None].double()
+    u0 = case["u"].double().cpu()
+    rng = np.random.default_rng(5)
+    eps = 1e-3
+    worst = 0.0
+    for _ in range(64):
+        vu = torch.from_numpy(rng.standard_normal(u0.shape)) * known
+        vl = float(rng.standard_normal()) * (0.01 if method == "nlpoisson" else 0.0)
+        vs = float(rng.standard_normal())
+        with torch.no_grad():
+            lp, _ = ref64(case, method, lam + eps * vl, sigma + eps * vs, u=u0 + eps * vu)
+            lm, _ = ref64(case, method, lam - eps * vl, sigma - eps * vs, u=u0 - eps * vu)
+        fd = float(lp - lm) / (2 * eps)
+        terms = (float((gu * vu).sum()), gl * vl, gs * vs)
+        an = sum(terms)
+        # relative to the size of the directional terms: a random direction
+        # can make the image and sigma parts cancel almost exactly
+        scale = max(abs(fd), sum(abs(t) for t in terms), 1e-9)
+        worst = max(worst, abs(an - fd) / scale)
+    print("48x48 %s: worst relative error over 64 directions %.3g" % (method, worst))
+    assert worst < 1e-4, worst
+
+
+@pytest.mark.parametrize("method", ["nlmeans", "nlpoisson"])
+def test_full_size_512_finite_differences(gpu_ctx, method):
+    """The differentiation workload at full size: 512x512 Voronoi image,
+    ~15% ellipse hole, NNF from a seeded PatchMatch run, lambda 0.05,
+    sigma 10000; gradients against FP64 central differences (step 1e-3,
+    sparse FP64 solve) along 16 random directions over (known pixels,
+    lambda, sigma)."""
+    sigma, lam = 10000.0, 0.05
+    case = make_case(gpu_ctx, 512, 4, method, sigma=sigma)
+    _, gu, gl, gs = ours(gpu_ctx, case, lam, sigma)
+    known = torch.from_numpy(case["mask"] == 0)[..., None].double()
+    u0 = case["u"].double().cpu()
+    rng = np.random.default_rng(6)
+    eps = 1e-3
+    worst = 0.0
+    for _ in range(16):
+        vu = torch.from_numpy(rng.standard_normal(u0.shape)) * known
+        vl = float(rng.standard_normal()) * (0.01 if method == "nlpoisson" else 0.0)
+        vs = float(rng.standard_normal()) * 1e3
+        with torch.no_grad():
+            lp, _ = ref64(case, method, lam + eps * vl, sigma + eps * vs, u=u0 + eps * vu, solver="sparse")
+            lm, _ = ref64(case, method, lam - eps * vl, sigma - eps * vs, u=u0 - eps * vu, solver="sparse")
+        fd = float(lp - lm) / (2 * eps)
+        terms = (float((gu * vu).sum()), gl * vl, gs * vs)
+        scale = max(abs(fd), sum(abs(t) for t in terms), 1e-9)
+        worst = max(worst, abs(sum(terms) - fd) / scale)
+    print("512x512 %s: worst relative error over 16 directions %.3g" % (method, worst))
+    assert worst < 1e-4, worst
