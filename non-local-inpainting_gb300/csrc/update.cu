@@ -278,6 +278,89 @@ __global__ void __launch_bounds__(128) k_poisson_coef(UpdArgs u, const int32_t *
 		gather_coef(u, x, y - 1, ext, nnf, conf, img, grad, out);
 }
 
+// The same gather with 8 lanes per coefficient pixel: item (k, which) is
+// hole pixel k itself (which 0), its left neighbour (1) or its upper
+// neighbour (2) when that pixel is owned as in k_poisson_coef; lane j of
+// the item's 8 takes window taps j, j + 8, ...; the 8 partial sums are
+// added with shuffles.  Same terms as gather_coef, summed in a tree.
+__global__ void __launch_bounds__(256) k_poisson_coef8(UpdArgs u, const int32_t *__restrict__ hole, int nh,
+                                                       const uint8_t *__restrict__ dom,
+                                                       const uint8_t *__restrict__ ext, const int2 *__restrict__ nnf,
+                                                       const float *__restrict__ conf, const float *__restrict__ img,
+                                                       const float2 *__restrict__ grad, CoefOut out)
+{
+	const int item = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+	const int sub = threadIdx.x & 7;
+	const int W = u.W, H = u.H, C = u.C;
+	bool owned = false;
+	int qx = 0, qy = 0;
+	if (item < 3 * nh) {
+		const int k = item / 3, which = item - 3 * k;
+		const int pix = hole[k];
+		const int x = pix % W, y = pix / W;
+		if (which == 0) {
+			owned = true;
+			qx = x;
+			qy = y;
+		} else if (which == 1) {
+			owned = x > 0 && !dom[pix - 1];
+			qx = x - 1;
+			qy = y;
+		} else {
+			owned = y > 0 && !dom[pix - W] && !(x + 1 < W && dom[pix - W + 1]);
+			qx = x;
+			qy = y - 1;
+		}
+	}
+	// all 8 lanes of an item agree on `owned`; whole groups leave together
+	if (!owned) return;
+	const unsigned gmask = 0xffu << (threadIdx.x & 24);
+	float S = 0.f, U[4] = {0, 0, 0, 0}, GX[4] = {0, 0, 0, 0}, GY[4] = {0, 0, 0, 0};
+	const int taps = u.px * u.py;
+	for (int t = sub; t < taps; t += 8) {
+		const int ty = t / u.px, tx = t - ty * u.px;
+		// centre c = q - (tap offset), tap offset = (tx - hx, ty - hy)
+		const int cx = qx - (tx - u.hx), cy = qy - (ty - u.hy);
+		if (cx < 0 || cy < 0 || cx >= W || cy >= H) continue;
+		const int c = cy * W + cx;
+		if (!ext[c]) continue;
+		const int2 nb = nnf[c];
+		const int nx = nb.x + qx - cx, ny = nb.y + qy - cy;
+		if (nx < 0 || ny < 0 || nx >= W || ny >= H) continue;
+		float w = u.weights[t];
+		if (conf) w = conf[c] * w;
+		S += w;
+		const float *iv = img + (size_t)C * (ny * W + nx);
+		const float2 *gv = grad + (size_t)C * (ny * W + nx);
+		for (int k = 0; k < C; k++) {
+			U[k] = fmaf(w, iv[k], U[k]);
+			const float2 g = gv[k];
+			GX[k] = fmaf(w, g.x, GX[k]);
+			GY[k] = fmaf(w, g.y, GY[k]);
+		}
+	}
+#pragma unroll
+	for (int o = 4; o > 0; o >>= 1) {
+		S += __shfl_xor_sync(gmask, S, o);
+#pragma unroll
+		for (int k = 0; k < 4; k++) {
+			if (k >= C) break;
+			U[k] += __shfl_xor_sync(gmask, U[k], o);
+			GX[k] += __shfl_xor_sync(gmask, GX[k], o);
+			GY[k] += __shfl_xor_sync(gmask, GY[k], o);
+		}
+	}
+	if (sub == 0) {
+		const int q = qy * W + qx;
+		out.S[q] = S;
+		for (int k = 0; k < C; k++) {
+			out.U[(size_t)C * q + k] = U[k];
+			out.GX[(size_t)C * q + k] = GX[k];
+			out.GY[(size_t)C * q + k] = GY[k];
+		}
+	}
+}
+
 // Per unknown (hole pixel) data of the symmetric system
 //   (a1 - div a2 grad) delta = b,  delta = 0 outside the hole,
 // with the anisotropic Laplacian of calculate_anisotropic_laplacian
@@ -867,8 +950,15 @@ static PoissonSystem poisson_system(nli_ctx *ctx, const UpdArgs &u, const nli_up
 	P.co.GY = ctx->buf<float>("poi.GY", n * C);
 	{
 		ProfScope ps(ctx, "poisson_coef");
-		k_poisson_coef<<<(nh + 127) / 128, 128, 0, s>>>(u, hole, nh, dom, ext, nnf, conf, image,
-		                                                 reinterpret_cast<const float2 *>(grad), P.co);
+		if (u.px % 2 == 1 && u.py % 2 == 1) {
+			const long long threads = 3LL * nh * 8;
+			k_poisson_coef8<<<(int)((threads + 255) / 256), 256, 0, s>>>(
+			    u, hole, nh, dom, ext, nnf, conf, image, reinterpret_cast<const float2 *>(grad), P.co);
+		} else {
+			// even patch sides: the window of gather_coef is one wider than the patch
+			k_poisson_coef<<<(nh + 127) / 128, 128, 0, s>>>(u, hole, nh, dom, ext, nnf, conf, image,
+			                                                 reinterpret_cast<const float2 *>(grad), P.co);
+		}
 		NLI_CHECK_LAUNCH();
 	}
 	PoissonArgs &pa = P.pa;
