@@ -274,6 +274,18 @@ int nli_patchmatch(nli_ctx *ctx, const nli_distance_params *dist, const nli_patc
                    const float *target, const uint8_t *target_mask, int tW, int tH, int C,
                    const int32_t *init_nnf, int32_t *out_nnf, float *out_distance, double *energy);
 
+/* PatchMatch::calculate as built with METRICS (patch_match.cpp:383-507,
+ * 574-590): nli_patchmatch plus, per sweep (pm->iterations entries), the
+ * sum of the matched distances after the sweep (total_distance) and the
+ * number of target points the propagation step improved (propagations),
+ * and the largest index of a first accepted random draw over the call
+ * (*max_random_shots).  Each output may be NULL. */
+int nli_patchmatch_metrics(nli_ctx *ctx, const nli_distance_params *dist, const nli_patchmatch_params *pm,
+                           const float *source, const uint8_t *source_mask, int sW, int sH,
+                           const float *target, const uint8_t *target_mask, int tW, int tH, int C,
+                           const int32_t *init_nnf, int32_t *out_nnf, float *out_distance, double *energy,
+                           double *total_distance, int64_t *propagations, int32_t *max_random_shots);
+
 /* ---- image updating (L2b) ------------------------------------------------ */
 /* AImageUpdating::update (a_image_updating.h:34-39): updates `image` in
  * place on `domain`, returns sum over domain of (old - new)^2.  `orig` may
@@ -315,6 +327,44 @@ int nli_process(nli_ctx *ctx, const nli_process_params *params,
 int nli_process_device(nli_ctx *ctx, const nli_process_params *params,
                        const float *image, const uint8_t *mask, int W, int H, int C,
                        float *out, nli_process_stats *stats);
+
+/* ImageInpainting::keep_intermediate (image_inpainting.cpp:310-313): while
+ * enabled, each nli_process / nli_process_device call on this context keeps
+ * host copies of its pyramids, replaced by the next call:
+ *   NLI_INTER_INPUT  per level (index 0 = finest) the image after
+ *                    downsampling, before the coarsest initialisation
+ *                    (get_input_image_pyramid, :103-108, 316-319);
+ *   NLI_INTER_OUTPUT per level the inpainted image (get_output_image_pyramid);
+ *   NLI_INTER_MASK   per level the hole mask, one byte per pixel (get_mask_pyramid);
+ *   NLI_INTER_NNF    the final NNF of every level in the order the levels
+ *                    are inpainted, coarsest first, W*H int32 pairs
+ *                    (get_nnf_pyramid, :410-412).
+ * Batches do not keep intermediates. */
+#define NLI_INTER_INPUT 0
+#define NLI_INTER_OUTPUT 1
+#define NLI_INTER_MASK 2
+#define NLI_INTER_NNF 3
+int nli_ctx_keep_intermediate(nli_ctx *ctx, int enable);
+/* Number of kept entries of `kind`. */
+int nli_intermediate_count(nli_ctx *ctx, int kind);
+/* Entry `index` of `kind`: sizes in *W, *H, *C (C is 1 for masks and 2 for
+ * NNFs); when host_out is not NULL, its W*H*C elements (floats, bytes or
+ * int32) are copied there. */
+int nli_intermediate_get(nli_ctx *ctx, int kind, int index, int *W, int *H, int *C, void *host_out);
+
+/* ---- colour and channel packing of the command-line caller ------------- */
+/* IOUtility::rgb_to_lab (io_utility.cpp:268-289, 380-412): sRGB in 0..255,
+ * 3 channels, to CIE L*a*b* (D65).  Device pointers, W*H pixels. */
+int nli_rgb_to_lab(nli_ctx *ctx, const float *rgb, int W, int H, float *lab);
+/* IOUtility::lab_to_rgb (io_utility.cpp:292-318, 415-449): the first three
+ * channels of a C-channel (3 or 4) L*a*b* image to sRGB 0..255 (3 channels). */
+int nli_lab_to_rgb(nli_ctx *ctx, const float *lab, int W, int H, int C, float *rgb);
+/* IOUtility::cat (io_utility.cpp:452-470): RGB (3 channels) and depth (1)
+ * into one 4-channel image. */
+int nli_cat_depth(nli_ctx *ctx, const float *rgb, const float *depth, int W, int H, float *rgbd);
+/* IOUtility::separate (io_utility.cpp:489-501): the reverse; rgb or depth
+ * may be NULL. */
+int nli_separate_depth(nli_ctx *ctx, const float *rgbd, int W, int H, float *rgb, float *depth);
 
 /* ---- batched driver ------------------------------------------------------ */
 /* Many independent image/mask pairs on one GPU.  The reference has no batch

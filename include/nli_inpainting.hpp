@@ -333,14 +333,20 @@ public:
 		p.window = _window;
 		return p;
 	}
-	/* The sweeps run in parallel on the GPU: the energy after the last sweep
-	 * is the one entry of the per-iteration vector. */
+	/* The figures of the reference's METRICS build for the last calculate()
+	 * (patch_match.cpp:383-507): per sweep the sum of the matched distances
+	 * and the number of points the propagation improved, and the largest
+	 * index of a first accepted random draw. */
 	std::vector<double> get_total_distance_per_iteration() { return _energy; }
+	std::vector<int> get_propagations_per_iteration_metric() { return _propagations; }
+	int get_max_random_shots_count() { return _max_shots; }
 
 private:
 	APatchDistance *_d;
 	int _iters, _window, _shots;
 	std::vector<double> _energy;
+	std::vector<int> _propagations;
+	int _max_shots = 0;
 };
 
 /* ------------------------------------------------------ a_image_updating.h */
@@ -443,6 +449,13 @@ public:
 	void set_image_updating(AImageUpdating *u) { _upd = u; }
 	/* Per-scale iteration counts etc. of the last process() call. */
 	const nli_process_stats &get_statistics() const { return _stats; }
+	/* Keep the pyramids of the next process() calls
+	 * (image_inpainting.cpp:103-108, 310-337, 410-412). */
+	void keep_intermediate(bool value = true) { _keep = value; }
+	std::vector<Image<float> > get_input_image_pyramid() { return _input_pyr; }
+	std::vector<Image<float> > get_output_image_pyramid() { return _output_pyr; }
+	std::vector<Mask> get_mask_pyramid() { return _mask_pyr; }
+	std::vector<Image<Point> > get_nnf_pyramid() { return _nnf_pyr; }
 
 private:
 	PatchMatch *_pm;
@@ -453,6 +466,10 @@ private:
 	float _rate, _conft, _confa;
 	InitType _init;
 	nli_process_stats _stats;
+	bool _keep = false;
+	std::vector<Image<float> > _input_pyr, _output_pyr;
+	std::vector<Mask> _mask_pyr;
+	std::vector<Image<Point> > _nnf_pyr;
 };
 
 #endif /* NLI_INPAINTING_HPP_ */

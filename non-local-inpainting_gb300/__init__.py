@@ -87,6 +87,15 @@ def load(path=LIB_PATH):
     proto("nli_bruteforce_nnf", I, [P, dp, P, P, I, I, P, P, I, I, I, P, P])
     proto("nli_patchmatch", I, [P, dp, pp, P, P, I, I, P, P, I, I, I, P, P, P, ct.POINTER(ct.c_double)])
     proto("nli_update", I, [P, up, P, P, P, P, P, P, I, I, I, ct.POINTER(ct.c_double)])
+    proto("nli_patchmatch_metrics", I, [P, dp, pp, P, P, I, I, P, P, I, I, I, P, P, P, ct.POINTER(ct.c_double),
+                                        P, P, ct.POINTER(ct.c_int32)])
+    proto("nli_rgb_to_lab", I, [P, P, I, I, P])
+    proto("nli_lab_to_rgb", I, [P, P, I, I, I, P])
+    proto("nli_cat_depth", I, [P, P, P, I, I, P])
+    proto("nli_separate_depth", I, [P, P, I, I, P, P])
+    proto("nli_ctx_keep_intermediate", I, [P, I])
+    proto("nli_intermediate_count", I, [P, I])
+    proto("nli_intermediate_get", I, [P, I, I, ct.POINTER(I), ct.POINTER(I), ct.POINTER(I), P])
     proto("nli_update_backward", I, [P, up, P, P, P, P, P, P, I, I, I, P, P, ct.POINTER(ct.c_double),
                                      ct.POINTER(ct.c_double), ct.POINTER(ct.c_double)])
     proto("nli_process", I, [P, prp, P, P, I, I, I, P, st])
@@ -320,6 +329,80 @@ class Context:
         self._check(self.lib.nli_update(self.h, ct.byref(upd), _ptr(img), _ptr(org), _ptr(dom), _ptr(ext), _ptr(nnf),
                                         _ptr(conf), W, H, C, ct.byref(tot)))
         return img, tot.value
+
+    def patchmatch_metrics(self, dist, pm, src, smask, tgt, tmask, init=None):
+        """PatchMatch with the reference's METRICS figures: returns (nnf,
+        distance, energy, total distance per sweep, propagations per sweep,
+        max random-shot index)."""
+        src, tgt, smask, tmask = self._f32(src), self._f32(tgt), self._u8(smask), self._u8(tmask)
+        init = None if init is None else self._i32(init)
+        sW, sH, C = _dims(src)
+        tW, tH, _ = _dims(tgt)
+        nnf = self._empty((tH, tW, 2), self.torch.int32)
+        d = self._empty((tH, tW), self.torch.float32)
+        n = max(pm.iterations, 1)
+        tot = (ct.c_double * n)()
+        prop = (ct.c_int64 * n)()
+        e, shots = ct.c_double(), ct.c_int32()
+        self._check(self.lib.nli_patchmatch_metrics(self.h, ct.byref(dist), ct.byref(pm), _ptr(src), _ptr(smask), sW,
+                                                    sH, _ptr(tgt), _ptr(tmask), tW, tH, C, _ptr(init), _ptr(nnf),
+                                                    _ptr(d), ct.byref(e), tot, prop, ct.byref(shots)))
+        k = pm.iterations
+        return nnf, d, e.value, list(tot)[:k], list(prop)[:k], shots.value
+
+    def rgb_to_lab(self, rgb):
+        """IOUtility::rgb_to_lab on the GPU (sRGB 0..255, 3 channels)."""
+        rgb = self._f32(rgb)
+        W, H, _ = _dims(rgb)
+        out = self._empty((H, W, 3), self.torch.float32)
+        self._check(self.lib.nli_rgb_to_lab(self.h, _ptr(rgb), W, H, _ptr(out)))
+        return out
+
+    def lab_to_rgb(self, lab):
+        """IOUtility::lab_to_rgb on the GPU (3 or 4 channels in, 3 out)."""
+        lab = self._f32(lab)
+        W, H, C = _dims(lab)
+        out = self._empty((H, W, 3), self.torch.float32)
+        self._check(self.lib.nli_lab_to_rgb(self.h, _ptr(lab), W, H, C, _ptr(out)))
+        return out
+
+    def cat_depth(self, rgb, depth):
+        rgb, depth = self._f32(rgb), self._f32(depth)
+        W, H, _ = _dims(rgb)
+        out = self._empty((H, W, 4), self.torch.float32)
+        self._check(self.lib.nli_cat_depth(self.h, _ptr(rgb), _ptr(depth), W, H, _ptr(out)))
+        return out
+
+    def separate_depth(self, rgbd):
+        rgbd = self._f32(rgbd)
+        W, H, _ = _dims(rgbd)
+        rgb = self._empty((H, W, 3), self.torch.float32)
+        depth = self._empty((H, W), self.torch.float32)
+        self._check(self.lib.nli_separate_depth(self.h, _ptr(rgbd), W, H, _ptr(rgb), _ptr(depth)))
+        return rgb, depth
+
+    INTER_INPUT, INTER_OUTPUT, INTER_MASK, INTER_NNF = 0, 1, 2, 3
+
+    def keep_intermediate(self, enable=True):
+        """ImageInpainting::keep_intermediate for the next process() calls."""
+        self._check(self.lib.nli_ctx_keep_intermediate(self.h, 1 if enable else 0))
+
+    def intermediate(self, kind):
+        """Kept pyramid of `kind` (INTER_INPUT / OUTPUT / MASK: per level,
+        finest first; INTER_NNF: per inpainted level, coarsest first) as
+        numpy arrays."""
+        count = self.lib.nli_intermediate_count(self.h, kind)
+        if count < 0:
+            raise NliError(count, "bad intermediate kind")
+        dtype = {0: np.float32, 1: np.float32, 2: np.uint8, 3: np.int32}[kind]
+        out = []
+        for i in range(count):
+            W, H, C = I(), I(), I()
+            self._check(self.lib.nli_intermediate_get(self.h, kind, i, ct.byref(W), ct.byref(H), ct.byref(C), None))
+            a = np.empty((H.value, W.value, C.value), dtype)
+            self._check(self.lib.nli_intermediate_get(self.h, kind, i, None, None, None, a.ctypes.data_as(P)))
+            out.append(a[..., 0] if kind == 2 else a)
+        return out
 
     def update_backward(self, upd, image, out, dom, ext, nnf, conf, grad_out):
         """Adjoint of update(upd, image, image, ...) with the NNF fixed:

@@ -15,7 +15,7 @@ DROPIN = os.path.join(HERE, "libnli_dropin.so")
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
 SOURCES = ["api.cu", "gradient.cu", "distance.cu", "patchmatch.cu", "update.cu", "pyramid.cu", "process.cu",
-           "batch.cu"]
+           "batch.cu", "color.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-I", os.path.join(ROOT, "include"), "-I", CSRC]
@@ -66,6 +66,7 @@ def build(force=False, verbose=False, extra=()):
         _run([nvcc, *ARCH, "-shared", *objs, "-o", LIB + ".tmp", "-lcudart"])
         os.replace(LIB + ".tmp", LIB)
     build_dropin(force)
+    build_cli(force)
     return LIB
 
 
@@ -80,6 +81,22 @@ def build_dropin(force=False):
           "-L", os.path.join(CUDA_HOME, "lib64"), "-lcudart", "-Wl,-rpath,$ORIGIN"])
     os.replace(DROPIN + ".tmp", DROPIN)
     return DROPIN
+
+
+CLI = os.path.join(HERE, "nli_inpaint")
+
+
+def build_cli(force=False):
+    """nli_inpaint: the reference's command-line program over the drop-in classes."""
+    src = os.path.join(CSRC, "cli.cpp")
+    deps = [src, LIB, DROPIN, os.path.join(ROOT, "include", "nli_inpainting.hpp"), os.path.join(ROOT, "include", "nli.h")]
+    if not force and not _stale(CLI, deps):
+        return CLI
+    _run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), "-I", os.path.join(CUDA_HOME, "include"),
+          src, "-o", CLI + ".tmp", "-L", HERE, "-lnli_dropin", "-lnli_gb300", "-L", os.path.join(CUDA_HOME, "lib64"),
+          "-lcudart", "-Wl,-rpath,$ORIGIN"])
+    os.replace(CLI + ".tmp", CLI)
+    return CLI
 
 
 if __name__ == "__main__":

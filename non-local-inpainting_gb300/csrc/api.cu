@@ -357,6 +357,81 @@ int nli_patchmatch(nli_ctx *ctx, const nli_distance_params *dist, const nli_patc
 	API_END(ctx)
 }
 
+int nli_patchmatch_metrics(nli_ctx *ctx, const nli_distance_params *dist, const nli_patchmatch_params *pm,
+                           const float *source, const uint8_t *source_mask, int sW, int sH, const float *target,
+                           const uint8_t *target_mask, int tW, int tH, int C, const int32_t *init_nnf,
+                           int32_t *out_nnf, float *out_distance, double *energy, double *total_distance,
+                           int64_t *propagations, int32_t *max_random_shots)
+{
+	API_BEGIN(ctx)
+	require_ptrs({dist, pm, source, source_mask, target, target_mask, out_nnf});
+	require_dims(sW, sH, C);
+	require_dims(tW, tH, C);
+	NLI_REQUIRE(pm->iterations >= 0 && pm->random_shots >= 0, NLI_E_INVALID, "negative PatchMatch parameter");
+	PatchMatchMetricsHost m;
+	double e = 0.0;
+	patchmatch_run(ctx, *dist, *pm, source, source_mask, sW, sH, target, target_mask, tW, tH, C, init_nnf, out_nnf,
+	               out_distance, &e, nullptr, -1, &m);
+	if (energy) *energy = e;
+	for (size_t i = 0; i < m.total_distance.size(); i++) {
+		if (total_distance) total_distance[i] = m.total_distance[i];
+		if (propagations) propagations[i] = m.propagations[i];
+	}
+	if (max_random_shots) *max_random_shots = m.max_random_shots;
+	API_END(ctx)
+}
+
+int nli_ctx_keep_intermediate(nli_ctx *ctx, int enable)
+{
+	if (!ctx) return NLI_E_INVALID;
+	ctx->keep_intermediate = enable != 0;
+	return NLI_OK;
+}
+
+int nli_intermediate_count(nli_ctx *ctx, int kind)
+{
+	if (!ctx) return NLI_E_INVALID;
+	switch (kind) {
+	case NLI_INTER_INPUT: return (int)ctx->inter_input.size();
+	case NLI_INTER_OUTPUT: return (int)ctx->inter_output.size();
+	case NLI_INTER_MASK: return (int)ctx->inter_mask.size();
+	case NLI_INTER_NNF: return (int)ctx->inter_nnf.size();
+	default: return NLI_E_INVALID;
+	}
+}
+
+int nli_intermediate_get(nli_ctx *ctx, int kind, int index, int *W, int *H, int *C, void *host_out)
+{
+	if (!ctx) return NLI_E_INVALID;
+	const nli_ctx::Kept *k = nullptr;
+	size_t elem = 0;
+	switch (kind) {
+	case NLI_INTER_INPUT:
+		if (index >= 0 && index < (int)ctx->inter_input.size()) k = &ctx->inter_input[index];
+		elem = sizeof(float);
+		break;
+	case NLI_INTER_OUTPUT:
+		if (index >= 0 && index < (int)ctx->inter_output.size()) k = &ctx->inter_output[index];
+		elem = sizeof(float);
+		break;
+	case NLI_INTER_MASK:
+		if (index >= 0 && index < (int)ctx->inter_mask.size()) k = &ctx->inter_mask[index];
+		elem = 1;
+		break;
+	case NLI_INTER_NNF:
+		if (index >= 0 && index < (int)ctx->inter_nnf.size()) k = &ctx->inter_nnf[index];
+		elem = sizeof(int32_t);
+		break;
+	default: break;
+	}
+	if (!k) return NLI_E_INVALID;
+	if (W) *W = k->W;
+	if (H) *H = k->H;
+	if (C) *C = k->C;
+	if (host_out) std::memcpy(host_out, k->data.data(), (size_t)k->W * k->H * k->C * elem);
+	return NLI_OK;
+}
+
 int nli_update(nli_ctx *ctx, const nli_update_params *upd, float *image, const float *orig, const uint8_t *domain,
                const uint8_t *ext_domain, const int32_t *nnf, const float *confidence, int W, int H, int C,
                double *total_difference)
@@ -408,6 +483,43 @@ int nli_update_backward(nli_ctx *ctx, const nli_update_params *upd, const float 
 	require_dims(W, H, C);
 	update_backward_run(ctx, *upd, image, out, domain, ext_domain, nnf, confidence, W, H, C, grad_out, grad_image,
 	                    grad_lambda, grad_lambda_d, grad_sigma);
+	API_END(ctx)
+}
+
+int nli_rgb_to_lab(nli_ctx *ctx, const float *rgb, int W, int H, float *lab)
+{
+	API_BEGIN(ctx)
+	require_ptrs({rgb, lab});
+	require_dims(W, H, 3);
+	rgb_to_lab_run(ctx, rgb, W * H, lab);
+	API_END(ctx)
+}
+
+int nli_lab_to_rgb(nli_ctx *ctx, const float *lab, int W, int H, int C, float *rgb)
+{
+	API_BEGIN(ctx)
+	require_ptrs({lab, rgb});
+	require_dims(W, H, C);
+	NLI_REQUIRE(C == 3 || C == 4, NLI_E_CHANNELS, "lab_to_rgb takes 3 or 4 channels");
+	lab_to_rgb_run(ctx, lab, W * H, C, rgb);
+	API_END(ctx)
+}
+
+int nli_cat_depth(nli_ctx *ctx, const float *rgb, const float *depth, int W, int H, float *rgbd)
+{
+	API_BEGIN(ctx)
+	require_ptrs({rgb, depth, rgbd});
+	require_dims(W, H, 4);
+	cat_depth_run(ctx, rgb, depth, W * H, rgbd);
+	API_END(ctx)
+}
+
+int nli_separate_depth(nli_ctx *ctx, const float *rgbd, int W, int H, float *rgb, float *depth)
+{
+	API_BEGIN(ctx)
+	require_ptrs({rgbd});
+	require_dims(W, H, 4);
+	separate_depth_run(ctx, rgbd, W * H, rgb, depth);
 	API_END(ctx)
 }
 

@@ -169,12 +169,19 @@ Image<Point> PatchMatch::calculate(FixedImage<float> source, FixedMask source_ma
 	nli_patchmatch_params pm = gpu_params();
 	double energy = 0.0;
 	const float *sp = s->as<float>();
-	check(nli_patchmatch(default_context(), &dp, &pm, sp, sm->as<uint8_t>(), sW, sH, t ? t->as<float>() : sp,
-	                     tm->as<uint8_t>(), tW, tH, C, init ? init->as<int32_t>() : nullptr, out.as<int32_t>(), nullptr,
-	                     &energy));
+	std::vector<double> total((size_t)std::max(_iters, 1));
+	std::vector<int64_t> prop((size_t)std::max(_iters, 1));
+	int32_t shots = 0;
+	check(nli_patchmatch_metrics(default_context(), &dp, &pm, sp, sm->as<uint8_t>(), sW, sH,
+	                             t ? t->as<float>() : sp, tm->as<uint8_t>(), tW, tH, C,
+	                             init ? init->as<int32_t>() : nullptr, out.as<int32_t>(), nullptr, &energy,
+	                             total.data(), prop.data(), &shots));
 	Image<Point> nnf(tW, tH, Point(-1, -1));
 	download(nnf.raw(), out, sizeof(Point) * (size_t)tW * tH);
-	_energy.assign(1, energy);
+	const size_t sweeps = (size_t)std::max(_iters, 0);
+	_energy.assign(total.begin(), total.begin() + sweeps);
+	_propagations.assign(prop.begin(), prop.begin() + sweeps);
+	_max_shots = shots;
 	return nnf;
 }
 
@@ -252,7 +259,40 @@ Image<float> ImageInpainting::process(FixedImage<float> in, FixedMask mask)
 	p.conf_asymptotic = _confa;
 	p.init = (int32_t)_init;
 	Image<float> out(in.get_size_x(), in.get_size_y(), in.get_number_of_channels());
-	check(nli_process(default_context(), &p, in.raw(), mask.bytes(), in.get_size_x(), in.get_size_y(),
-	                  in.get_number_of_channels(), out.raw(), &_stats));
+	nli_ctx *ctx = default_context();
+	check(nli_ctx_keep_intermediate(ctx, _keep ? 1 : 0));
+	check(nli_process(ctx, &p, in.raw(), mask.bytes(), in.get_size_x(), in.get_size_y(), in.get_number_of_channels(),
+	                  out.raw(), &_stats));
+	_input_pyr.clear();
+	_output_pyr.clear();
+	_mask_pyr.clear();
+	_nnf_pyr.clear();
+	if (_keep) {
+		int W, H, C;
+		for (int kind : {NLI_INTER_INPUT, NLI_INTER_OUTPUT}) {
+			for (int i = 0; i < nli_intermediate_count(ctx, kind); i++) {
+				check(nli_intermediate_get(ctx, kind, i, &W, &H, &C, nullptr));
+				Image<float> im((uint)W, (uint)H, (uint)C);
+				check(nli_intermediate_get(ctx, kind, i, nullptr, nullptr, nullptr, im.raw()));
+				(kind == NLI_INTER_INPUT ? _input_pyr : _output_pyr).push_back(im);
+			}
+		}
+		for (int i = 0; i < nli_intermediate_count(ctx, NLI_INTER_MASK); i++) {
+			check(nli_intermediate_get(ctx, NLI_INTER_MASK, i, &W, &H, &C, nullptr));
+			std::vector<uint8_t> b((size_t)W * H);
+			check(nli_intermediate_get(ctx, NLI_INTER_MASK, i, nullptr, nullptr, nullptr, b.data()));
+			Mask m((uint)W, (uint)H);
+			for (int y = 0; y < H; y++)
+				for (int x = 0; x < W; x++)
+					if (b[(size_t)y * W + x]) m.mask((uint)x, (uint)y);
+			_mask_pyr.push_back(m);
+		}
+		for (int i = 0; i < nli_intermediate_count(ctx, NLI_INTER_NNF); i++) {
+			check(nli_intermediate_get(ctx, NLI_INTER_NNF, i, &W, &H, &C, nullptr));
+			Image<Point> nnf((uint)W, (uint)H, Point(-1, -1));
+			check(nli_intermediate_get(ctx, NLI_INTER_NNF, i, nullptr, nullptr, nullptr, nnf.raw()));
+			_nnf_pyr.push_back(nnf);
+		}
+	}
 	return out;
 }

@@ -107,6 +107,14 @@ struct nli_ctx {
 	};
 	bool profiling = false;
 	std::map<std::string, ProfEntry> prof;
+	// ImageInpainting::keep_intermediate: host copies of the last process()'s
+	// pyramids (image_inpainting.cpp:103-108, 316-337, 410-412)
+	struct Kept {
+		int W = 0, H = 0, C = 0;
+		std::vector<unsigned char> data;
+	};
+	bool keep_intermediate = false;
+	std::vector<Kept> inter_input, inter_output, inter_mask, inter_nnf;
 	// batched processing (batch.cu): images in flight and their worker contexts
 	int batch_width = 8;
 	std::vector<nli_ctx *> workers;
@@ -204,11 +212,17 @@ void launch_sum_partials(cudaStream_t s, const double *partials, int n, double *
 struct PmStats {
 	double energy;
 };
+// Per-sweep figures of the reference's METRICS build (patch_match.cpp:383-507).
+struct PatchMatchMetricsHost {
+	std::vector<double> total_distance;   // per sweep
+	std::vector<int64_t> propagations;    // per sweep
+	int max_random_shots = 0;
+};
 void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patchmatch_params &pm,
                     const float *src, const uint8_t *smask, int sW, int sH, const float *tgt,
                     const uint8_t *tmask, int tW, int tH, int C, const int32_t *init_nnf,
                     int32_t *out_nnf, float *out_dist, double *energy, const int32_t *tlist = nullptr,
-                    int n_target = -1);
+                    int n_target = -1, PatchMatchMetricsHost *metrics = nullptr);
 
 // update.cu
 double update_run(nli_ctx *ctx, const nli_update_params &up, float *image, const float *orig,
@@ -244,6 +258,12 @@ void process_batch_run(nli_ctx *ctx, int n, const nli_process_params *params, co
                        const uint8_t *const *masks, const int32_t *widths, const int32_t *heights,
                        const int32_t *channels, float *const *outputs, nli_process_stats *stats, int32_t *status,
                        bool host_buffers);
+
+// color.cu
+void rgb_to_lab_run(nli_ctx *ctx, const float *rgb, int n, float *lab);
+void lab_to_rgb_run(nli_ctx *ctx, const float *lab, int n, int C, float *rgb);
+void cat_depth_run(nli_ctx *ctx, const float *rgb, const float *depth, int n, float *out);
+void separate_depth_run(nli_ctx *ctx, const float *rgbd, int n, float *rgb, float *depth);
 
 // process.cu
 void process_run(nli_ctx *ctx, const nli_process_params &p, const float *img, const uint8_t *mask, int W,

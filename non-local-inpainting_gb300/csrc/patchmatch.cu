@@ -425,16 +425,21 @@ __global__ void __launch_bounds__(1024, 1) k_pm_init(DistArgs a, PmArgs p, const
 	}
 }
 
+// metric_prop (may be NULL): this sweep's count of target points that the
+// propagation step improved; metric_shots (may be NULL): the largest index
+// of a first accepted random draw (patch_match.cpp:452-456, 481-485).
 template <int KIND, int C, int P>
 __global__ void __launch_bounds__(1024, 1) k_pm_sweep(DistArgs a, PmArgs p, int sweep, int jump,
                                                        const int2 *__restrict__ nnf_in, const float *__restrict__ dist_in,
                                                        int2 *__restrict__ nnf_out, float *__restrict__ dist_out,
-                                                       unsigned long long *counter)
+                                                       unsigned long long *counter, unsigned long long *metric_prop,
+                                                       int *metric_shots)
 {
 	const int lane = threadIdx.x & 31;
 	const PmSmem m = pm_smem(a, p);
 	load_weights(a, m.w);
-	unsigned evals = 0, partial = 0;
+	unsigned evals = 0, partial = 0, improved = 0;
+	int max_shot = -1;
 	// number of random-search windows: max_window, max_window / 2, ..., 1
 	const int windows = 32 - __clz(p.max_window);
 	const int chunk = (p.nt + gridDim.x - 1) / gridDim.x;
@@ -467,7 +472,9 @@ __global__ void __launch_bounds__(1024, 1) k_pm_sweep(DistArgs a, PmArgs p, int 
 			int mycand;
 			int n = compact_candidates(valid, packed, best, m.list, mycand);
 			evals += n;
+			const float bd_before = bd;
 			eval_candidates<KIND, C, P>(p, m.w, m.t, mycand, n, best, bd, partial);
+			if (bd < bd_before) improved++;
 			// random search around the match after propagation: lane k draws
 			// in window max_window >> k from its own stream, up to `shots`
 			// draws, and proposes the first that lands in the source
@@ -484,6 +491,7 @@ __global__ void __launch_bounds__(1024, 1) k_pm_sweep(DistArgs a, PmArgs p, int 
 					if (src_ok(p, rx, ry)) {
 						valid = true;
 						packed = rx | (ry << 16);
+						max_shot = max(max_shot, t);
 						break;
 					}
 				}
@@ -504,6 +512,11 @@ __global__ void __launch_bounds__(1024, 1) k_pm_sweep(DistArgs a, PmArgs p, int 
 	if (lane == 0 && evals) {
 		atomicAdd(counter, (unsigned long long)evals);
 		if (partial) atomicAdd(counter + 1, (unsigned long long)partial);
+	}
+	if (metric_prop && lane == 0 && improved) atomicAdd(metric_prop, (unsigned long long)improved);
+	if (metric_shots) {
+		max_shot = __reduce_max_sync(kFull, max_shot);
+		if (lane == 0 && max_shot >= 0) atomicMax(metric_shots, max_shot);
 	}
 }
 
@@ -549,9 +562,21 @@ static int jump_for(int sweep, int tW, int tH)
 	return j;
 }
 
+// Device buffers of the METRICS build's per-sweep figures (NULL: not kept).
+struct PmMetrics {
+	double *energy = nullptr;              // per sweep: sum of matched distances
+	unsigned long long *prop = nullptr;    // per sweep: points improved by propagation
+	int *shots = nullptr;                  // largest accepted draw index
+	double *partials = nullptr;            // scratch of the energy reduction
+	int partial_blocks = 0;
+};
+
+static void sweep_energy(cudaStream_t s, const PmArgs &p, const float *dist, const PmMetrics &m, int sweep);
+
 template <int KIND, int C, int P>
 static void run_sweeps(nli_ctx *ctx, const DistArgs &a, const PmArgs &p, int iterations, const int2 *init,
-                       int2 *nnf_x, float *dist_x, int2 *nnf_y, float *dist_y, unsigned long long *counter)
+                       int2 *nnf_x, float *dist_x, int2 *nnf_y, float *dist_y, unsigned long long *counter,
+                       const PmMetrics &mt)
 {
 	// persistent: one 32-warp block per SM (fewer when there are fewer points)
 	const int block = 1024;
@@ -569,15 +594,23 @@ static void run_sweeps(nli_ctx *ctx, const DistArgs &a, const PmArgs &p, int ite
 		ProfScope ps(ctx, "pm_sweep");
 		k_pm_sweep<KIND, C, P><<<grid, block, smem, ctx->stream>>>(
 		    a, p, it, jump_for(it, p.tW, p.tH), even ? nnf_x : nnf_y, even ? dist_x : dist_y, even ? nnf_y : nnf_x,
-		    even ? dist_y : dist_x, counter);
+		    even ? dist_y : dist_x, counter, mt.prop ? mt.prop + it : nullptr, mt.shots);
 		NLI_CHECK_LAUNCH();
+		if (mt.energy) sweep_energy(ctx->stream, p, even ? dist_y : dist_x, mt, it);
 	}
+}
+
+static void sweep_energy(cudaStream_t s, const PmArgs &p, const float *dist, const PmMetrics &m, int sweep)
+{
+	k_energy<<<m.partial_blocks, 256, 0, s>>>(p.tlist, p.nt, dist, m.partials);
+	NLI_CHECK_LAUNCH();
+	launch_sum_partials(s, m.partials, m.partial_blocks, m.energy + sweep);
 }
 
 void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patchmatch_params &pm, const float *src,
                     const uint8_t *smask, int sW, int sH, const float *tgt, const uint8_t *tmask, int tW, int tH,
                     int C, const int32_t *init_nnf, int32_t *out_nnf, float *out_dist, double *energy,
-                    const int32_t *tlist, int n_target)
+                    const int32_t *tlist, int n_target, PatchMatchMetricsHost *metrics)
 {
 	DistArgs a;
 	fill_dist_args(a, dp, C);
@@ -643,14 +676,25 @@ void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patch
 		const uint64_t k = ctx->seed ^ (call * 0x9E3779B97F4A7C15ULL);
 		p.key = make_uint2((uint32_t)k, (uint32_t)(k >> 32) ^ (uint32_t)call);
 		if (energy) NLI_CUDA(cudaMemsetAsync(counter, 0, 2 * sizeof(unsigned long long), s));
+		PmMetrics mt;
+		const int iters = std::max(pm.iterations, 0);
+		if (metrics && iters > 0) {
+			mt.energy = ctx->buf<double>("pm.m_energy", iters);
+			mt.prop = ctx->buf<unsigned long long>("pm.m_prop", iters);
+			mt.shots = ctx->buf<int>("pm.m_shots", 1);
+			mt.partial_blocks = std::min((n_target + 255) / 256, 1024);
+			mt.partials = ctx->buf<double>("pm.m_partials", mt.partial_blocks + 1);
+			NLI_CUDA(cudaMemsetAsync(mt.prop, 0, sizeof(unsigned long long) * iters, s));
+			NLI_CUDA(cudaMemsetAsync(mt.shots, 0, sizeof(int), s));
+		}
 		// 9 x 9 patches (the reference's default) have their rows unrolled
 		const bool p9 = a.px == 9 && a.py == 9;
 #define NLI_PM_CASE(KIND, CC)                                                                                \
 	if (dp.kind == KIND && C == CC) {                                                                            \
 		if (p9)                                                                                                  \
-			run_sweeps<KIND, CC, 9>(ctx, a, p, pm.iterations, init, nnf_x, dist_x, nnf_y, dist_y, counter); \
+			run_sweeps<KIND, CC, 9>(ctx, a, p, pm.iterations, init, nnf_x, dist_x, nnf_y, dist_y, counter, mt); \
 		else                                                                                                     \
-			run_sweeps<KIND, CC, 0>(ctx, a, p, pm.iterations, init, nnf_x, dist_x, nnf_y, dist_y, counter); \
+			run_sweeps<KIND, CC, 0>(ctx, a, p, pm.iterations, init, nnf_x, dist_x, nnf_y, dist_y, counter, mt); \
 		handled = true;                                                                                          \
 	}
 		bool handled = false;
@@ -689,6 +733,17 @@ void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patch
 			ctx->candidates += (int64_t)hc[0];
 			ctx->candidates_partial += (int64_t)hc[1];
 			*energy = *reinterpret_cast<double *>(hc + 2);
+		}
+		if (metrics && iters > 0) {
+			metrics->total_distance.resize(iters);
+			std::vector<unsigned long long> prop(iters);
+			NLI_CUDA(cudaMemcpyAsync(metrics->total_distance.data(), mt.energy, sizeof(double) * iters,
+			                         cudaMemcpyDeviceToHost, s));
+			NLI_CUDA(cudaMemcpyAsync(prop.data(), mt.prop, sizeof(unsigned long long) * iters, cudaMemcpyDeviceToHost,
+			                         s));
+			NLI_CUDA(cudaMemcpyAsync(&metrics->max_random_shots, mt.shots, sizeof(int), cudaMemcpyDeviceToHost, s));
+			NLI_CUDA(cudaStreamSynchronize(s));
+			metrics->propagations.assign(prop.begin(), prop.end());
 		}
 	} else if (energy) {
 		*energy = 0.0;

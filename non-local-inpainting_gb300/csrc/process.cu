@@ -108,6 +108,19 @@ struct Driver {
 
 	std::string tag(int l, const char *what) { return "proc." + std::to_string(l) + "." + what; }
 
+	// host copy of a device buffer for keep_intermediate
+	static nli_ctx::Kept keep(nli_ctx *ctx, const void *dev, int W, int H, int C, size_t elem)
+	{
+		nli_ctx::Kept k;
+		k.W = W;
+		k.H = H;
+		k.C = C;
+		k.data.resize((size_t)W * H * C * elem);
+		NLI_CUDA(cudaMemcpyAsync(k.data.data(), dev, k.data.size(), cudaMemcpyDeviceToHost, ctx->stream));
+		NLI_CUDA(cudaStreamSynchronize(ctx->stream));
+		return k;
+	}
+
 	void prepare(int l)
 	{
 		Level &L = lv[l];
@@ -173,6 +186,7 @@ struct Driver {
 			stats->iterations[l] = i;
 			stats->last_difference[l] = total;
 		}
+		if (ctx->keep_intermediate) ctx->inter_nnf.push_back(keep(ctx, nnf, L.W, L.H, 2, sizeof(int32_t)));
 		return const_cast<int32_t *>(nnf);
 	}
 
@@ -257,6 +271,16 @@ struct Driver {
 				                    lv[i].mask);
 			}
 		}
+		if (ctx->keep_intermediate) {
+			ctx->inter_input.clear();
+			ctx->inter_output.clear();
+			ctx->inter_mask.clear();
+			ctx->inter_nnf.clear();
+			for (int i = 0; i < S; i++) {
+				ctx->inter_input.push_back(keep(ctx, lv[i].img, lv[i].W, lv[i].H, C, sizeof(float)));
+				ctx->inter_mask.push_back(keep(ctx, lv[i].mask, lv[i].W, lv[i].H, 1, 1));
+			}
+		}
 		// coarsest initialisation (:111-155)
 		Level &top = lv[S - 1];
 		if (p.init == NLI_INIT_AVG || p.init == NLI_INIT_BLACK) {
@@ -274,6 +298,9 @@ struct Driver {
 			nnf = inpaint(i, nnf);
 		}
 		NLI_CUDA(cudaMemcpyAsync(out, lv[0].img, (size_t)W * H * C * sizeof(float), cudaMemcpyDeviceToDevice, s));
+		if (ctx->keep_intermediate)
+			for (int i = 0; i < S; i++)
+				ctx->inter_output.push_back(keep(ctx, lv[i].img, lv[i].W, lv[i].H, C, sizeof(float)));
 		unsigned long long *hc = reinterpret_cast<unsigned long long *>(ctx->host_pinned);
 		NLI_CUDA(cudaMemcpyAsync(hc, counter, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
 		NLI_CUDA(cudaStreamSynchronize(s));

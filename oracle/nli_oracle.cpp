@@ -1675,6 +1675,65 @@ int orc_poisson_init(float *img, const uint8_t *mask, int W, int H, int C)
 	return NLI_OK;
 }
 
+/* Colour conversions of the command-line caller, restated from
+ * io_utility.cpp:380-449 (sRGB <-> XYZ <-> L*a*b*, D65 white), keeping its
+ * float / double evaluation order and its float pow. */
+static float orc_srgb_expand(float v)
+{
+	return (v > 0.04045) ? std::pow((v + 0.055f) / 1.055f, 2.4f) : v / 12.92;
+}
+
+static float orc_lab_f(float t) { return (t > 0.008856f) ? std::pow(t, 1.0f / 3.0f) : (7.787f * t) + (16.0f / 116.0f); }
+
+int orc_rgb_to_lab(const float *rgb, int W, int H, float *lab)
+{
+	for (long i = 0; i < (long)W * H; i++) {
+		const float *c = rgb + 3 * i;
+		float r = orc_srgb_expand(c[0] / 255.0f), g = orc_srgb_expand(c[1] / 255.0f), b = orc_srgb_expand(c[2] / 255.0f);
+		r *= 100.0f;
+		g *= 100.0f;
+		b *= 100.0f;
+		const float X = r * 0.412453f + g * 0.357580f + b * 0.180423f;
+		const float Y = r * 0.212671f + g * 0.715160f + b * 0.072169f;
+		const float Z = r * 0.019334f + g * 0.119193f + b * 0.950227f;
+		const float fx = orc_lab_f(X / 95.047f), fy = orc_lab_f(Y / 100.000f), fz = orc_lab_f(Z / 108.883f);
+		lab[3 * i] = (116.0f * fy) - 16.0f;
+		lab[3 * i + 1] = 500.0f * (fx - fy);
+		lab[3 * i + 2] = 200.0f * (fy - fz);
+	}
+	return NLI_OK;
+}
+
+static float orc_lab_finv(float t)
+{
+	const float t3 = std::pow(t, 3.0f);
+	return (t3 > 0.008856f) ? t3 : (t - 16.0f / 116.0f) / 7.787f;
+}
+
+static float orc_srgb_compress(float v)
+{
+	return (v > 0.0031308f) ? 1.055f * std::pow(v, 1.0f / 2.4f) - 0.055f : 12.92f * v;
+}
+
+int orc_lab_to_rgb(const float *lab, int W, int H, int C, float *rgb)
+{
+	for (long i = 0; i < (long)W * H; i++) {
+		const float *c = lab + (long)C * i;
+		const float fy = (c[0] + 16.0f) / 116.0f;
+		const float fx = c[1] / 500.0 + fy;
+		const float fz = fy - c[2] / 200.0f;
+		const float X = orc_lab_finv(fx) * 95.047f, Y = orc_lab_finv(fy) * 100.000f, Z = orc_lab_finv(fz) * 108.883f;
+		const float x = X / 100.0f, y = Y / 100.0f, z = Z / 100.0f;
+		const float r = x * 3.240479f + y * -1.537150f + z * -0.498535f;
+		const float g = x * -0.969256f + y * 1.875992f + z * 0.041556f;
+		const float b = x * 0.055648f + y * -0.204043f + z * 1.057311f;
+		rgb[3 * i] = orc_srgb_compress(r) * 255.0f;
+		rgb[3 * i + 1] = orc_srgb_compress(g) * 255.0f;
+		rgb[3 * i + 2] = orc_srgb_compress(b) * 255.0f;
+	}
+	return NLI_OK;
+}
+
 float orc_subsampling_rate(float ratio, unsigned scales)
 {
 	/* float overloads of exp/log, as the reference resolves them */

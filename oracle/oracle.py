@@ -79,6 +79,8 @@ class _Lib:
         self._sm = proto("scale_masks", I, [P, I, I, I, I, P, P, ct.POINTER(I)])
         self._pinit = proto("poisson_init", I, [P, P, I, I, I])
         self._rate = proto("subsampling_rate", F, [F, ct.c_uint])
+        self._rgb2lab = proto("rgb_to_lab", I, [P, I, I, P])
+        self._lab2rgb = proto("lab_to_rgb", I, [P, I, I, I, P])
         proc_args = [ct.c_uint] + ([I] if self.parallel_arg else []) + [prp, P, P, I, I, I, P] + (
             [ct.POINTER(_abi.ProcessStats)] if self.parallel_arg else [])
         self._proc = proto("process", I, proc_args)
@@ -207,6 +209,18 @@ class _Lib:
 
     def subsampling_rate(self, ratio, scales):
         return self._rate(ratio, scales)
+
+    def rgb_to_lab(self, rgb):
+        rgb = _f32(rgb)
+        out = np.empty(rgb.shape[:2] + (3,), np.float32)
+        self._check(self._rgb2lab(_ptr(rgb), rgb.shape[1], rgb.shape[0], _ptr(out)), "rgb_to_lab")
+        return out
+
+    def lab_to_rgb(self, lab):
+        lab = _f32(lab)
+        out = np.empty(lab.shape[:2] + (3,), np.float32)
+        self._check(self._lab2rgb(_ptr(lab), lab.shape[1], lab.shape[0], lab.shape[2], _ptr(out)), "lab_to_rgb")
+        return out
 
 
 class Oracle(_Lib):

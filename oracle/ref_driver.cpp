@@ -45,6 +45,7 @@
 #include "patch_non_local_poisson.h"
 #include "patch_non_local_depth.h"
 #include "image_inpainting.h"
+#include "io_utility.h"
 #undef private
 #undef protected
 
@@ -336,6 +337,25 @@ int ref_poisson_init(float *img, const uint8_t *mask, int W, int H, int C)
 	for (int c = 0; c < C; c++)
 		for (int j = 0; j < H; j++)
 			for (int i = 0; i < W; i++) img[C * (W * j + i) + c] = out[i + j * W + c * W * H];
+	return 0;
+}
+
+/* IOUtility::rgb_to_lab / lab_to_rgb (io_utility.cpp:268-318) on W*H pixels. */
+int ref_rgb_to_lab(const float *rgb, int W, int H, float *lab)
+{
+	Image<float> in((unsigned)W, (unsigned)H, 3u);
+	std::memcpy(in.raw(), rgb, sizeof(float) * 3 * W * H);
+	Image<float> out = IOUtility::rgb_to_lab(in);
+	std::memcpy(lab, out.raw(), sizeof(float) * 3 * W * H);
+	return 0;
+}
+
+int ref_lab_to_rgb(const float *lab, int W, int H, int C, float *rgb)
+{
+	Image<float> in((unsigned)W, (unsigned)H, (unsigned)C);
+	std::memcpy(in.raw(), lab, sizeof(float) * C * W * H);
+	Image<float> out = IOUtility::lab_to_rgb(in);
+	std::memcpy(rgb, out.raw(), sizeof(float) * 3 * W * H);
 	return 0;
 }
 

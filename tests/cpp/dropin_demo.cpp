@@ -70,7 +70,11 @@ int main(int argc, char **argv)
 		PatchMatch *patch_match = new PatchMatch(distance, 10, 30, -1);
 		inpainting.set_weights_updating(patch_match);
 		inpainting.set_image_updating(updating);
+		inpainting.keep_intermediate(true);
 		Image<float> output = inpainting.process(input, mask);
+		printf("pyramid levels %zu masks %zu nnfs %zu finest nnf %ux%u\n", inpainting.get_output_image_pyramid().size(),
+		       inpainting.get_mask_pyramid().size(), inpainting.get_nnf_pyramid().size(),
+		       inpainting.get_nnf_pyramid().back().get_size_x(), inpainting.get_nnf_pyramid().back().get_size_y());
 
 		FILE *f = fopen(argv[7], "wb");
 		fwrite(output.raw(), sizeof(float), (size_t)W * H * C, f);
@@ -98,7 +102,10 @@ int main(int argc, char **argv)
 					source.unmask(x, y);
 				}
 		Image<Point> nnf = patch_match->calculate(output, source, output, target);
-		printf("patchmatch energy %.6g\n", patch_match->get_total_distance_per_iteration()[0]);
+		printf("patchmatch energy per sweep %.6g .. %.6g, propagations in sweep 1: %d\n",
+		       patch_match->get_total_distance_per_iteration().front(),
+		       patch_match->get_total_distance_per_iteration().back(),
+		       patch_match->get_propagations_per_iteration_metric().front());
 		Point t0 = target.get_masked_points()[0];
 		printf("distance %.6g\n", distance->calculate(nnf(t0), t0));
 		Image<float> copy = output.clone();

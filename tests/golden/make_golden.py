@@ -137,6 +137,19 @@ def unit_cases(ref):
     # coarsest Poisson fill
     g["pinit_in"], g["pinit_mask"] = g["down_img_0"], g["down_mask_0"]
     g["pinit_out"] = ref.poisson_init(g["down_img_0"], g["down_mask_0"])
+    # colour conversions of the command-line caller: every 8-bit grey level
+    # and seeded random colours (0..255) through rgb_to_lab and back
+    lrng = np.random.default_rng(77)
+    lv = np.arange(256, dtype=np.float32)
+    rgb = np.concatenate([np.stack([lv, lv, lv], -1)[None], lrng.uniform(0, 255, (1, 256, 3)).astype(np.float32),
+                          np.round(lrng.uniform(0, 255, (1, 256, 3))).astype(np.float32)], axis=1)
+    g["lab_rgb_in"] = rgb
+    g["lab_out"] = ref.rgb_to_lab(rgb)
+    g["lab_rgb_back"] = ref.lab_to_rgb(g["lab_out"])
+    # a 4-channel (L*a*b* + depth) input: the reference's lab_to_rgb reads its
+    # separated copy after that copy is destroyed (io_utility.cpp:303-307),
+    # so its output is not stored; the intended result drops the depth
+    g["lab4_in"] = np.concatenate([g["lab_out"], lrng.uniform(0.5, 5, rgb.shape[:2] + (1,)).astype(np.float32)], -1)
     # PatchMatch + updates on one 64x64 scale
     img, mask, p = wl.config1(seed=21, size=64)
     ext = ref.extended_domain(mask, 9, 9)

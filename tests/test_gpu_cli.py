@@ -1,0 +1,131 @@
+"""The command-line caller of the path: colour conversions on the GPU
+against the reference's (golden vectors), RGB-D packing, and nli_inpaint
+(main.cpp's program on the drop-in classes) against the same steps driven
+through the C ABI."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import __graft_entry__ as ge
+from conftest import ROOT
+
+pytestmark = pytest.mark.gpu
+CLI = os.path.join(ROOT, "non-local-inpainting_gb300", "nli_inpaint")
+
+
+def test_lab_conversions(gpu_ctx, units):
+    # the GPU evaluates the reference's float pow as a double pow rounded to float
+    lab = gpu_ctx.rgb_to_lab(units["lab_rgb_in"]).cpu().numpy()
+    assert np.abs(lab - units["lab_out"]).max() <= 1e-4
+    back = gpu_ctx.lab_to_rgb(units["lab_out"]).cpu().numpy()
+    assert np.abs(back - units["lab_rgb_back"]).max() <= 1e-3
+    assert np.abs(back - units["lab_rgb_in"]).max() <= 0.02  # the round trip
+    # a depth channel is dropped (the reference's own 4-channel path reads
+    # freed memory, io_utility.cpp:303-307)
+    back4 = gpu_ctx.lab_to_rgb(units["lab4_in"]).cpu().numpy()
+    assert np.array_equal(back4, back)
+
+
+def test_depth_packing(gpu_ctx):
+    rng = np.random.default_rng(1)
+    rgb = rng.uniform(0, 255, (13, 17, 3)).astype(np.float32)
+    depth = rng.uniform(0.5, 5, (13, 17)).astype(np.float32)
+    rgbd = gpu_ctx.cat_depth(rgb, depth).cpu().numpy()
+    assert np.array_equal(rgbd, np.concatenate([rgb, depth[..., None]], -1))
+    r, d = gpu_ctx.separate_depth(rgbd)
+    assert np.array_equal(r.cpu().numpy(), rgb) and np.array_equal(d.cpu().numpy(), depth)
+
+
+def write_pnm(path, a):
+    a = np.clip(np.round(a), 0, 255).astype(np.uint8)
+    H, W = a.shape[:2]
+    with open(path, "wb") as f:
+        f.write(b"P6\n" if a.ndim == 3 else b"P5\n")
+        f.write(b"%d %d\n255\n" % (W, H))
+        f.write(a.tobytes())
+
+
+def read_pnm(path):
+    with open(path, "rb") as f:
+        data = f.read()
+    parts = data.split(b"\n", 3)
+    W, H = map(int, parts[1].split())
+    C = 3 if parts[0] == b"P6" else 1
+    return np.frombuffer(parts[3], np.uint8).reshape(H, W, C)
+
+
+@pytest.fixture(scope="module")
+def cli():
+    ge.build()
+    assert os.path.exists(CLI)
+    return CLI
+
+
+def test_cli_matches_c_abi(cli, gpu_ctx, tmp_path):
+    from nli_gb300 import workloads as wl
+    img, mask, _ = wl.config2(seed=8, size=72, scales=3)
+    img8 = np.clip(np.round(img), 0, 255)
+    write_pnm(tmp_path / "in.ppm", img8)
+    write_pnm(tmp_path / "mask.pgm", mask * 255)
+    r = subprocess.run([cli, "in.ppm", "mask.pgm", "out", "-method", "nlmeans", "-patch", "9", "-scales", "3",
+                        "-coarse", "0.5", "-iters", "10", "-seed", "5", "-shownnf", "nnf.ppm", "-showpyr", "pyr_"],
+                       cwd=tmp_path, capture_output=True, text=True)
+    print(r.stdout, r.stderr)
+    assert r.returncode == 0, r.stderr
+    name = "out_nlmeans_sc3_0.5_initnone_ps9_10000_conf5_0.1.ppm"  # main.cpp's composed name
+    assert name in r.stdout
+    got = read_pnm(tmp_path / name)
+    # the same steps through the C ABI: Lab, process with the CLI's pairing
+    # (nlmeans with L2Norm distances), back to RGB, rounded
+    p = wl.params("nlmeans", distance="l2", patch=9, scales=3, coarse=0.5, iters=10)
+    p.patchmatch.random_shots = 30
+    lab = gpu_ctx.rgb_to_lab(img8.astype(np.float32)).cpu().numpy()
+    gpu_ctx.set_seed(5)
+    out, _ = gpu_ctx.process(lab, mask, p)
+    v = gpu_ctx.lab_to_rgb(out).cpu().numpy().astype(np.float64)
+    v = np.where(v >= 0, np.floor(v + 0.5), np.ceil(v - 0.5))  # std::round: halves away from zero
+    want = np.clip(v, 0, 255).astype(np.uint8)
+    assert np.array_equal(got, want)
+    known = mask == 0
+    assert np.abs(got[known].astype(int) - img8[known].astype(int)).max() <= 1  # Lab round trip
+    for n in range(3):
+        assert (tmp_path / ("pyr_%d.ppm" % n)).exists()
+    nnf_img = read_pnm(tmp_path / "nnf.ppm")
+    assert nnf_img.shape == got.shape and (nnf_img == 0).any()
+
+
+def test_cli_errors(cli, tmp_path):
+    img = np.full((40, 40, 3), 100.0)
+    write_pnm(tmp_path / "in.ppm", img)
+    write_pnm(tmp_path / "mask.pgm", np.zeros((40, 40)))
+    r = subprocess.run([cli, "in.ppm", "mask.pgm", "out"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode != 0 and "ERROR: Mask should not be empty (all black)" in r.stderr
+    write_pnm(tmp_path / "mask2.pgm", np.ones((30, 40)) * 255)
+    r = subprocess.run([cli, "in.ppm", "mask2.pgm", "out"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode != 0 and "ERROR: Input image and mask should be of the same size" in r.stderr
+    r = subprocess.run([cli, "in.ppm"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 1 and "USAGE" in r.stderr
+
+
+def test_cli_depth(cli, tmp_path):
+    from nli_gb300 import workloads as wl
+    img, mask, _ = wl.config3(seed=2, w=80, h=64, scales=3)
+    write_pnm(tmp_path / "in.ppm", img[..., :3])
+    write_pnm(tmp_path / "mask.pgm", mask * 255)
+    d = img[..., 3]
+    with open(tmp_path / "depth.pfm", "wb") as f:
+        f.write(b"Pf\n%d %d\n-1.0\n" % (d.shape[1], d.shape[0]))
+        f.write(np.ascontiguousarray(d[::-1]).astype("<f4").tobytes())
+    r = subprocess.run([cli, "in.ppm", "mask.pgm", "out", "-method", "nldepth", "-depth", "depth.pfm", "-lambdar", "1.0",
+                        "-lambdad", "0.0", "-patch", "9", "-scales", "3", "-coarse", "0.5", "-iters", "5", "-seed", "1"],
+                       cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    with open(tmp_path / "inpainted_depth.pfm", "rb") as f:
+        raw = f.read()
+    hdr = raw.split(b"\n", 3)
+    out_d = np.frombuffer(hdr[3], "<f4").reshape(d.shape)[::-1]
+    known = mask == 0
+    assert np.array_equal(out_d[known], d[known])  # known depth untouched
+    assert np.isfinite(out_d).all() and (out_d[~known] > 0.3).all()

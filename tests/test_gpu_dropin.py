@@ -61,3 +61,4 @@ def test_dropin_program_matches_c_abi(demo, gpu_ctx, tmp_path, method):
     ref, _ = gpu_ctx.process(img, mask, params_for(method))
     assert np.array_equal(out, ref)
     assert "size mismatch gives empty field: 1" in r.stdout
+    assert "pyramid levels 3 masks 3 nnfs 3 finest nnf %dx%d" % (W, H) in r.stdout

@@ -86,6 +86,16 @@ def test_updates(oracle, units):
     assert np.array_equal(out, units["upd_3"]) and tot == float(units["upd_3_total"])
 
 
+def test_lab_conversions(oracle, units):
+    """io_utility.cpp:268-318 restated: bit-exact with the reference on every
+    grey level and seeded colours, both directions.  With a depth channel the
+    reference reads freed memory (io_utility.cpp:303-307); the restatement
+    drops the depth channel, as that code intends."""
+    assert np.array_equal(oracle.rgb_to_lab(units["lab_rgb_in"]), units["lab_out"])
+    assert np.array_equal(oracle.lab_to_rgb(units["lab_out"]), units["lab_rgb_back"])
+    assert np.array_equal(oracle.lab_to_rgb(units["lab4_in"]), units["lab_rgb_back"])
+
+
 def test_bruteforce(oracle, units):
     nnf, d = oracle.bruteforce_nnf(dparams(0), units["bf_img"], units["bf_src"], units["bf_img"], units["bf_tgt"])
     assert np.array_equal(nnf, units["bf_nnf"]) and np.array_equal(d, units["bf_dist"])
