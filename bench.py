@@ -412,12 +412,23 @@ def batch_compare(pkg, ctx, args, local):
     tb = timed(batched)
     plain()
     tp = timed(plain)
+
+    def kernel_ms(fn):
+        # one more pass with per-kernel CUDA events (outside the timed passes)
+        ctx.set_profiling(True)
+        fn()
+        prof = ctx.profile()
+        ctx.set_profiling(False)
+        return {k: round(v[1], 1) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
+
+    kb, kp = kernel_ms(batched), kernel_ms(plain)
     return {"workload": "uneven batch: %d images, sides log-uniform 128-%d, aspect 0.5-2, 5-30%% ellipse/stroke "
                         "holes, nlmeans/nlpoisson alternating, patch 9, scales |round(log(0.1 size)/log(0.75))|, "
                         "automatic coarsest rate (seed 5)" % (len(items), args.batch_max_side),
             "mpix": mpix, "plain_mpix_s": mpix / tp, "batched_mpix_s": mpix / tb, "speedup": tp / tb,
             "plain_s": tp, "batched_s": tb, "batch_width": args.batch_width, "gpu_launches": int(launches),
             "identical_to_plain": all(bool(torch.equal(x, y)) for x, y in zip(outs, ref)),
+            "kernel_ms_plain": kp, "kernel_ms_batched": kb,
             "scales": [p.scales for p in params]}
 
 

@@ -293,16 +293,53 @@ __global__ void k_dt_rows(const float *__restrict__ g, int W, int H, int *__rest
 	}
 }
 
+// The row pass as a bounded search, one thread per pixel.  Both passes work
+// on exact integers (column distances, squared offsets), so the row result
+// is min over u of (x - u)^2 + g(u)^2 whatever the order of evaluation; the
+// lower envelope above finds it for a whole row at once, this search looks
+// outward from x while d^2 is below the best value found (any farther u
+// cannot do better).  The final square root is rounded as dt_f rounds it,
+// so both give the same floats; the search keeps every SM busy.
+__global__ void k_dt_rows_search(const float *__restrict__ g, int W, int H, float *__restrict__ out)
+{
+	const size_t n = (size_t)W * H;
+	for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+		const int x = (int)(i % W);
+		const float *gy = g + (i - x);
+		const unsigned long long gx = (unsigned long long)gy[x];
+		unsigned long long best = gx * gx;
+		for (unsigned long long d = 1; d * d < best; d++) {
+			const bool lo = (long long)x - (long long)d >= 0, hi = x + d < (unsigned long long)W;
+			if (!lo && !hi) break;
+			if (lo) {
+				const unsigned long long gu = (unsigned long long)gy[x - d];
+				best = min(best, d * d + gu * gu);
+			}
+			if (hi) {
+				const unsigned long long gu = (unsigned long long)gy[x + d];
+				best = min(best, d * d + gu * gu);
+			}
+		}
+		out[i] = best ? __double2float_rn(__dsqrt_rn((double)best)) : 0.0f;
+	}
+}
+
 void distance_transform_run(nli_ctx *ctx, const uint8_t *mask, int W, int H, float *out)
 {
 	float *g = ctx->buf<float>("dt.g", (size_t)W * H);
-	int *sb = ctx->buf<int>("dt.s", (size_t)W * H);
-	int *tb = ctx->buf<int>("dt.t", (size_t)W * H);
 	const float INF = (float)((unsigned)W + (unsigned)H);
 	k_dt_columns<<<(W + 31) / 32, 32, 0, ctx->stream>>>(mask, W, H, INF, g);
 	NLI_CHECK_LAUNCH();
-	// one row per thread, 32 rows per block: the rows spread over the SMs
-	k_dt_rows<<<(H + 31) / 32, 32, 0, ctx->stream>>>(g, W, H, sb, tb, out);
+	// bounded search per pixel up to 4096 columns (its work grows with the
+	// hole's extent); the lower envelope, one thread per row, beyond
+	if (W <= 4096) {
+		const size_t n = (size_t)W * H;
+		k_dt_rows_search<<<(int)std::min<size_t>((n + 255) / 256, 65535), 256, 0, ctx->stream>>>(g, W, H, out);
+	} else {
+		int *sb = ctx->buf<int>("dt.s", (size_t)W * H);
+		int *tb = ctx->buf<int>("dt.t", (size_t)W * H);
+		k_dt_rows<<<(H + 31) / 32, 32, 0, ctx->stream>>>(g, W, H, sb, tb, out);
+	}
 	NLI_CHECK_LAUNCH();
 }
 
