@@ -390,6 +390,19 @@ int nli_process_batch_device(nli_ctx *ctx, int n, const nli_process_params *para
                              float *const *outputs, nli_process_stats *stats, int32_t *status);
 /* Images in flight in a batch (default 8, at least 1). */
 int nli_ctx_set_batch_width(nli_ctx *ctx, int width);
+
+/* Launch-shape knobs, set by the autotuner (non-local-inpainting_gb300/
+ * autotune.py) or by hand; results do not depend on them beyond float
+ * rounding of the CG sums:
+ *   NLI_TUNE_CG_CLUSTER_CAP        CTAs per CG cluster at most (1..16, default 16)
+ *   NLI_TUNE_CG_UNKNOWNS_PER_CTA   unknowns per CG CTA at least (default 1024)
+ *   NLI_TUNE_BATCH_WIDTH           as nli_ctx_set_batch_width
+ * nli_ctx_get_tuning reads them back. */
+#define NLI_TUNE_CG_CLUSTER_CAP 0
+#define NLI_TUNE_CG_UNKNOWNS_PER_CTA 1
+#define NLI_TUNE_BATCH_WIDTH 2
+int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value);
+int nli_ctx_get_tuning(nli_ctx *ctx, int knob, int *value);
 /* The seed image `index` of a batch runs with. */
 uint64_t nli_batch_seed(uint64_t seed, int index);
 

@@ -104,6 +104,8 @@ def load(path=LIB_PATH):
     proto("nli_process_batch_device", I, [P, I, prp, P, P, P, P, P, P, st, P])
     proto("nli_ctx_set_batch_width", I, [P, I])
     proto("nli_batch_seed", ct.c_uint64, [ct.c_uint64, I])
+    proto("nli_ctx_set_tuning", I, [P, I, I])
+    proto("nli_ctx_get_tuning", I, [P, I, ct.POINTER(I)])
     proto("nli_launch_count", ct.c_int64, [])
     proto("nli_ctx_set_profiling", I, [P, I])
     proto("nli_ctx_profile_entry", I, [P, I, ct.c_char_p, I, ct.POINTER(ct.c_int64), ct.POINTER(ct.c_double)])
@@ -477,6 +479,16 @@ class Context:
         self.last_batch_status = list(status)
         self._check(rc)
         return outs, [s.as_dict() for s in st]
+
+    TUNE_CG_CLUSTER_CAP, TUNE_CG_UNKNOWNS_PER_CTA, TUNE_BATCH_WIDTH = 0, 1, 2
+
+    def set_tuning(self, knob, value):
+        self._check(self.lib.nli_ctx_set_tuning(self.h, knob, value))
+
+    def get_tuning(self, knob):
+        v = I()
+        self._check(self.lib.nli_ctx_get_tuning(self.h, knob, ct.byref(v)))
+        return v.value
 
     def batch_seed(self, seed, index):
         return int(self.lib.nli_batch_seed(seed, index))

@@ -44,3 +44,20 @@ def image_update(nli, params, image, lam, sigma, dom, ext, nnf, conf=None, lam_d
     """One differentiable update step; lam, sigma (and lam_d) may be tensors
     with requires_grad."""
     return ImageUpdate.apply(image, lam, sigma, lam_d, nli, params, dom, ext, nnf, conf)
+
+
+def replay_updates(nli, params, image, lam, sigma, dom, ext, nnf, conf=None, steps=1, lam_d=None):
+    """`steps` update steps from `image` with one checkpointed NNF held fixed
+    (for instance a level's final NNF from Context.intermediate(INTER_NNF)),
+    each a differentiable image_update: gradients flow back through every
+    step to the starting image, lambda and sigma.  The backward pass
+    recomputes each step's weights and coefficients from the saved image;
+    only the images between steps are kept.  NL-Poisson steps here use the
+    step's own input as `orig`; the multiscale driver keeps the level's
+    start image there, which gives the same exact solution (the known
+    pixels, the only ones the solution reads outside the hole, never
+    change)."""
+    u = image
+    for _ in range(steps):
+        u = image_update(nli, params, u, lam, sigma, dom, ext, nnf, conf, lam_d)
+    return u

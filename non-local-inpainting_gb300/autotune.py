@@ -1,0 +1,88 @@
+"""Autotuner for the launch shapes the library leaves open: the size of the
+thread-block clusters of the NL-Poisson conjugate gradient (CTAs per
+cluster, unknowns per CTA) and the number of images a batch keeps in
+flight.  Each candidate is timed with CUDA events on a representative case
+on the context's own device; the fastest is set on the context
+(nli_ctx_set_tuning) and returned with the whole table, which callers may
+store and re-apply with apply().  Results depend on these shapes only
+through the float rounding of the CG's sums.
+"""
+from __future__ import annotations
+
+import itertools
+
+
+def _events(torch):
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def poisson_case(ctx, size=512, hole=0.15, seed=0):
+    """A finest-level NL-Poisson update case: Voronoi texture, ellipse hole,
+    NNF from a seeded PatchMatch call, confidence of the hole."""
+    import numpy as np
+    from . import workloads as wl
+    rng = np.random.default_rng(seed)
+    img, _ = wl.voronoi_texture(size, size, 40, rng)
+    mask = wl.ellipse_mask(size, size, 6, hole, rng)
+    p = wl.params("nlpoisson", scales=2, coarse=0.5, iters=1, cg_tol=1e-4)
+    ext = ctx.extended_domain(mask, 9, 9)
+    src, tgt, _ = ctx.scale_masks(ext, 4, True)
+    u = ctx.poisson_init(img, mask)
+    ctx.set_seed(seed)
+    nnf, _, _ = ctx.patchmatch(p.distance, p.patchmatch, u, src, u, tgt)
+    conf = ctx.confidence_mask(mask, 5.0, 0.1)
+    return p.update, u, mask, ext, nnf, conf
+
+
+def tune_cg(ctx, case=None, caps=(4, 8, 12, 16), per_cta=(512, 1024, 2048), repeats=3):
+    """Times one NL-Poisson update per (cluster cap, unknowns per CTA) and
+    keeps the fastest.  Returns {"best": (cap, per), "ms": {(cap, per): ms}}."""
+    import torch
+    upd, u, mask, ext, nnf, conf = case if case is not None else poisson_case(ctx)
+    times = {}
+    for cap, per in itertools.product(caps, per_cta):
+        ctx.set_tuning(ctx.TUNE_CG_CLUSTER_CAP, cap)
+        ctx.set_tuning(ctx.TUNE_CG_UNKNOWNS_PER_CTA, per)
+        ctx.update(upd, u, u, mask, ext, nnf, conf)  # warm
+        best = float("inf")
+        for _ in range(repeats):
+            torch.cuda.synchronize()
+            a, b = _events(torch)
+            a.record()
+            ctx.update(upd, u, u, mask, ext, nnf, conf)
+            b.record()
+            torch.cuda.synchronize()
+            best = min(best, a.elapsed_time(b))
+        times[(cap, per)] = best
+    choice = min(times, key=times.get)
+    ctx.set_tuning(ctx.TUNE_CG_CLUSTER_CAP, choice[0])
+    ctx.set_tuning(ctx.TUNE_CG_UNKNOWNS_PER_CTA, choice[1])
+    return {"best": choice, "ms": times}
+
+
+def tune_batch_width(ctx, items, params, widths=(2, 4, 8, 12, 16)):
+    """Times process_batch_device on device-resident `items` per batch width
+    and keeps the fastest.  Returns {"best": width, "ms": {width: ms}}."""
+    import torch
+    times = {}
+    for w in widths:
+        ctx.set_batch_width(w)
+        torch.cuda.synchronize()
+        a, b = _events(torch)
+        a.record()
+        ctx.process_batch_device(items, params)
+        b.record()
+        torch.cuda.synchronize()
+        times[w] = a.elapsed_time(b)
+    choice = min(times, key=times.get)
+    ctx.set_batch_width(choice)
+    return {"best": choice, "ms": times}
+
+
+def apply(ctx, cg=None, batch_width=None):
+    """Re-applies stored choices: cg = (cap, unknowns per CTA)."""
+    if cg is not None:
+        ctx.set_tuning(ctx.TUNE_CG_CLUSTER_CAP, int(cg[0]))
+        ctx.set_tuning(ctx.TUNE_CG_UNKNOWNS_PER_CTA, int(cg[1]))
+    if batch_width is not None:
+        ctx.set_batch_width(int(batch_width))

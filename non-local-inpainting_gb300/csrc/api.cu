@@ -560,4 +560,35 @@ int nli_ctx_set_batch_width(nli_ctx *ctx, int width)
 
 uint64_t nli_batch_seed(uint64_t seed, int index) { return batch_seed(seed, index); }
 
+int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value)
+{
+	if (!ctx) return NLI_E_INVALID;
+	switch (knob) {
+	case NLI_TUNE_CG_CLUSTER_CAP:
+		if (value < 1 || value > 16) return NLI_E_INVALID;
+		ctx->tune_cg_cluster_cap = value;
+		return NLI_OK;
+	case NLI_TUNE_CG_UNKNOWNS_PER_CTA:
+		if (value < 1) return NLI_E_INVALID;
+		ctx->tune_cg_unknowns_per_cta = value;
+		return NLI_OK;
+	case NLI_TUNE_BATCH_WIDTH:
+		if (value < 1) return NLI_E_INVALID;
+		ctx->batch_width = value;
+		return NLI_OK;
+	}
+	return NLI_E_INVALID;
+}
+
+int nli_ctx_get_tuning(nli_ctx *ctx, int knob, int *value)
+{
+	if (!ctx || !value) return NLI_E_INVALID;
+	switch (knob) {
+	case NLI_TUNE_CG_CLUSTER_CAP: *value = ctx->tune_cg_cluster_cap; return NLI_OK;
+	case NLI_TUNE_CG_UNKNOWNS_PER_CTA: *value = ctx->tune_cg_unknowns_per_cta; return NLI_OK;
+	case NLI_TUNE_BATCH_WIDTH: *value = ctx->batch_width; return NLI_OK;
+	}
+	return NLI_E_INVALID;
+}
+
 }  // extern "C"

@@ -117,6 +117,9 @@ struct nli_ctx {
 	std::vector<Kept> inter_input, inter_output, inter_mask, inter_nnf;
 	// batched processing (batch.cu): images in flight and their worker contexts
 	int batch_width = 8;
+	// tunable launch shapes (nli_ctx_set_tuning)
+	int tune_cg_cluster_cap = 16;        // CTAs per CG cluster at most
+	int tune_cg_unknowns_per_cta = 1024; // at least this many unknowns per CG CTA
 	std::vector<nli_ctx *> workers;
 	std::vector<cudaEvent_t> event_pool;
 

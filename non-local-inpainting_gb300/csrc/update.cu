@@ -995,7 +995,8 @@ static PoissonSystem poisson_system(nli_ctx *ctx, const UpdArgs &u, const nli_up
 		ctx->cg_cluster_max = std::min(maxc, kClusterMax);
 	}
 	if (ctx->cg_cluster_max >= 1) {
-		P.ncta = std::max(1, std::min(ctx->cg_cluster_max, (nh + 2 * kClusterBlock - 1) / (2 * kClusterBlock)));
+		const int per = std::max(1, ctx->tune_cg_unknowns_per_cta);
+		P.ncta = std::max(1, std::min(std::min(ctx->cg_cluster_max, ctx->tune_cg_cluster_cap), (nh + per - 1) / per));
 		P.chunk = (nh + P.ncta - 1) / P.ncta;
 		if ((size_t)kClusterVectors * P.chunk * sizeof(float) + P.chunk * sizeof(UnkC) > kSmemBudget ||
 		    P.chunk > kClusterMaxChunk)
@@ -1234,8 +1235,8 @@ __global__ void __launch_bounds__(256) k_means_backward(UpdArgs u, AdjArgs a, co
 // lambda S_k out_k + (1-lambda) sum_nb s_nb(k) (out_nb - out_k) (D = the
 // backward divergence of (GX, GY), s_up / s_left = S of that neighbour,
 // s_down / s_right = S_k), weighted by the adjoint solution z = A^-1 g on
-// the hole; the identity and boundary-coupling part of dL/du for pixels
-// outside the hole; and dL/dlambda per hole pixel.
+// the hole; the boundary-coupling part of dL/du for pixels outside the
+// hole; and dL/dlambda per hole pixel.
 struct AdjCoef {
 	float *dS;   // W*H
 	float *dU;   // W*H*C
@@ -1246,7 +1247,7 @@ struct AdjCoef {
 
 __global__ void k_poisson_adj_coef(PoissonArgs pa, CoefOut co, AdjCoef ad, const uint8_t *__restrict__ dom,
                                    const float *__restrict__ out, const float *__restrict__ z,
-                                   const float *__restrict__ g, double *__restrict__ gacc,
+                                   double *__restrict__ gacc,
                                    double *__restrict__ lam_part, int depth)
 {
 	__shared__ double red[2][8];
@@ -1304,14 +1305,15 @@ __global__ void k_poisson_adj_coef(PoissonArgs pa, CoefOut co, AdjCoef ad, const
 				else
 					dl += v;
 			} else {
-				// identity and the coupling into the hole's stencil:
-				// (1 - lambda) sum over hole neighbours k of z_k s_q(k)
-				double v = (double)g[o];
+				// the coupling into the hole's stencil, (1 - lambda) sum over
+				// hole neighbours k of z_k s_q(k) (the identity part, g, is
+				// already in gacc from k_adj_init)
+				double v = 0.0;
 				if (hd) v += (double)oml * z[o + (size_t)C * W] * co.S[q];       // q is the upper neighbour of k
 				if (hu) v += (double)oml * z[o - (size_t)C * W] * co.S[q - W];   // q is the lower neighbour
 				if (hr) v += (double)oml * z[o + C] * co.S[q];                   // q is the left neighbour
 				if (hl) v += (double)oml * z[o - C] * co.S[q - 1];               // q is the right neighbour
-				atomicAdd(gacc + o, v);
+				if (v != 0.0) atomicAdd(gacc + o, v);
 			}
 		}
 		if (act) ad.dS[q] = dS;
@@ -1473,7 +1475,7 @@ void update_backward_run(nli_ctx *ctx, const nli_update_params &up, const float 
 		ad.active = ctx->buf<uint8_t>("adj.active", n);
 		const int grid = (int)((n + 255) / 256);
 		double *lam_part = ctx->buf<double>("adj.lam", 2 * (size_t)grid);
-		k_poisson_adj_coef<<<grid, 256, 0, s>>>(P.pa, P.co, ad, dom, out, zimg, grad_out, gacc, lam_part,
+		k_poisson_adj_coef<<<grid, 256, 0, s>>>(P.pa, P.co, ad, dom, out, zimg, gacc, lam_part,
 		                                        up.method == NLI_UPDATE_DEPTH ? 1 : 0);
 		NLI_CHECK_LAUNCH();
 		const int grid2 = (int)((n + 127) / 128);

@@ -141,3 +141,58 @@ def test_full_size_512_finite_differences(gpu_ctx, method):
         worst = max(worst, abs(sum(terms) - fd) / scale)
     print("512x512 %s: worst relative error over 16 directions %.3g" % (method, worst))
     assert worst < 1e-4, worst
+
+
+@pytest.mark.parametrize("method", ["nlmeans", "nlpoisson"])
+def test_replayed_steps(gpu_ctx, method):
+    """Three update steps replayed with one checkpointed NNF: gradients
+    through the chain against the chained FP64 re-expression (autograd) and
+    FP64 central differences along 8 random directions."""
+    from nli_gb300.autograd import replay_updates
+    sigma, lam, steps = 3.0, 0.05, 3
+    case = make_case(gpu_ctx, 48, 23, method, sigma=sigma)
+    u = case["u"].detach().clone().requires_grad_(True)
+    lt = torch.tensor(lam, dtype=torch.float64, requires_grad=True)
+    st = torch.tensor(sigma, dtype=torch.float64, requires_grad=True)
+    out = replay_updates(gpu_ctx, case["p"].update, u, lt, st, case["mask"], case["ext"], case["nnf"], case["conf"],
+                         steps=steps)
+    loss = (((out - case["target"]) ** 2) * case["hole"][..., None]).sum()
+    loss.backward()
+    gu, gl, gs = u.grad.double().cpu(), float(lt.grad), float(st.grad)
+
+    nnf = case["nnf"].cpu().numpy().reshape(48, 48, 2)
+    dom = case["mask"] != 0
+    ext = case["ext"].cpu().numpy()
+    conf = case["conf"].double().cpu().numpy()
+    t = case["target"].double().cpu()
+
+    def f64(u0, l, s):
+        x = u0
+        for _ in range(steps):
+            x = update64.means(x, s, nnf, dom, conf) if method == "nlmeans" else \
+                update64.poisson(x, l, s, nnf, dom, ext, conf)
+        return (((x - t) ** 2) * torch.from_numpy(dom)[..., None]).sum()
+
+    u64 = case["u"].double().cpu().requires_grad_(True)
+    l64 = torch.tensor(lam, dtype=torch.float64, requires_grad=True)
+    s64 = torch.tensor(sigma, dtype=torch.float64, requires_grad=True)
+    f64(u64, l64, s64).backward()
+    assert rel(gu, u64.grad) < 1e-4, rel(gu, u64.grad)
+    if method == "nlpoisson":
+        assert abs(gl - float(l64.grad)) <= 1e-4 * abs(float(l64.grad))
+    assert abs(gs - float(s64.grad)) <= 1e-4 * abs(float(s64.grad))
+    rng = np.random.default_rng(8)
+    u0 = case["u"].double().cpu()
+    known = torch.from_numpy(~dom)[..., None].double()
+    eps, worst = 1e-3, 0.0
+    for _ in range(8):
+        vu = torch.from_numpy(rng.standard_normal(u0.shape)) * known
+        vl = float(rng.standard_normal()) * (0.01 if method == "nlpoisson" else 0.0)
+        vs = float(rng.standard_normal())
+        with torch.no_grad():
+            fd = float(f64(u0 + eps * vu, lam + eps * vl, sigma + eps * vs) -
+                       f64(u0 - eps * vu, lam - eps * vl, sigma - eps * vs)) / (2 * eps)
+        terms = (float((gu * vu).sum()), gl * vl, gs * vs)
+        worst = max(worst, abs(sum(terms) - fd) / max(abs(fd), sum(abs(x) for x in terms)))
+    print("%d replayed %s steps: worst relative error %.3g" % (steps, method, worst))
+    assert worst < 1e-4, worst

@@ -1,0 +1,37 @@
+"""The autotuner's CG launch shapes: every candidate gives the same update
+up to the rounding of the CG sums, and the chosen shape is applied."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def test_tune_cg(gpu_ctx):
+    from nli_gb300 import autotune
+    case = autotune.poisson_case(gpu_ctx, size=192, seed=3)
+    upd, u, mask, ext, nnf, conf = case
+    outs = {}
+    for cap, per in ((4, 512), (16, 1024), (16, 2048)):
+        autotune.apply(gpu_ctx, cg=(cap, per))
+        outs[(cap, per)] = gpu_ctx.update(upd, u, u, mask, ext, nnf, conf)[0].cpu().numpy()
+    ref = outs[(16, 1024)]
+    hole = mask != 0
+    for k, o in outs.items():
+        rel = np.abs(o[hole] - ref[hole]).max() / np.abs(ref[hole]).max()
+        assert rel < 1e-3, (k, rel)  # CG stopped at tolerance 1e-4 from different sum orders
+    res = autotune.tune_cg(gpu_ctx, case, caps=(4, 16), per_cta=(512, 1024), repeats=1)
+    assert res["best"] in res["ms"] and len(res["ms"]) == 4
+    assert gpu_ctx.get_tuning(gpu_ctx.TUNE_CG_CLUSTER_CAP) == res["best"][0]
+    assert gpu_ctx.get_tuning(gpu_ctx.TUNE_CG_UNKNOWNS_PER_CTA) == res["best"][1]
+    autotune.apply(gpu_ctx, cg=(16, 1024))  # back to the defaults for later tests
+
+
+def test_tuning_knobs_validate(gpu_ctx):
+    from nli_gb300 import NliError
+    with pytest.raises(NliError):
+        gpu_ctx.set_tuning(gpu_ctx.TUNE_CG_CLUSTER_CAP, 17)
+    with pytest.raises(NliError):
+        gpu_ctx.set_tuning(99, 1)
+    gpu_ctx.set_tuning(gpu_ctx.TUNE_BATCH_WIDTH, 5)
+    assert gpu_ctx.get_tuning(gpu_ctx.TUNE_BATCH_WIDTH) == 5
+    gpu_ctx.set_tuning(gpu_ctx.TUNE_BATCH_WIDTH, 8)
