@@ -421,7 +421,7 @@ def batch_compare(pkg, ctx, args, local):
         ctx.set_profiling(False)
         return {k: round(v[1], 1) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
 
-    kb, kp = kernel_ms(batched), kernel_ms(plain)
+    kb, kp = (kernel_ms(batched), kernel_ms(plain)) if args.batch_profile else (None, None)
     return {"workload": "uneven batch: %d images, sides log-uniform 128-%d, aspect 0.5-2, 5-30%% ellipse/stroke "
                         "holes, nlmeans/nlpoisson alternating, patch 9, scales |round(log(0.1 size)/log(0.75))|, "
                         "automatic coarsest rate (seed 5)" % (len(items), args.batch_max_side),
@@ -470,6 +470,8 @@ def main():
                     help="images in the batched-vs-plain comparison (0 skips it)")
     ap.add_argument("--batch-max-side", type=int, default=512)
     ap.add_argument("--batch-width", type=int, default=8)
+    ap.add_argument("--no-batch-profile", dest="batch_profile", action="store_false",
+                    help="skip the per-kernel profiled passes of the batch comparison")
     args = ap.parse_args()
     if args.case:
         return run_case(args)
