@@ -226,6 +226,8 @@ def run_ours(args):
     pkg = ge.package()
     ge.build() if not os.path.exists(pkg.LIB_PATH) else None
     ctx = pkg.Context(local)
+    if args.pm_variant is not None:
+        ctx.set_tuning(ctx.TUNE_PM_VARIANT, args.pm_variant)
     img, mask, p = workload()
     H, W, C = img.shape
     mpix = W * H / 1e6
@@ -439,6 +441,8 @@ def run_case(args):
     import torch
     pkg = ge.package()
     ctx = pkg.Context(0)
+    if args.pm_variant is not None:
+        ctx.set_tuning(ctx.TUNE_PM_VARIANT, args.pm_variant)
     ctx.set_seed(7)
     img, mask, p = workload()
     ext = ctx.extended_domain(mask, p.update.patch_x, p.update.patch_y)
@@ -466,6 +470,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--pm-variant", type=int, default=None, choices=[0, 1, 2],
+                    help="9x9 PatchMatch window reads: 0 target in shared memory + plain source loads, "
+                         "1 source windows staged by tensor copies, 2 target in registers "
+                         "(default: the library's)")
     ap.add_argument("--batch-count", type=int, default=16,
                     help="images in the batched-vs-plain comparison (0 skips it)")
     ap.add_argument("--batch-max-side", type=int, default=512)

@@ -397,10 +397,17 @@ int nli_ctx_set_batch_width(nli_ctx *ctx, int width);
  *   NLI_TUNE_CG_CLUSTER_CAP        CTAs per CG cluster at most (1..16, default 16)
  *   NLI_TUNE_CG_UNKNOWNS_PER_CTA   unknowns per CG CTA at least (default 1024)
  *   NLI_TUNE_BATCH_WIDTH           as nli_ctx_set_batch_width
+ *   NLI_TUNE_PM_VARIANT            how 9x9 PatchMatch reads candidate windows:
+ *                                  0 (default) target window in shared memory,
+ *                                  source rows by plain loads; 1 source windows
+ *                                  staged in shared memory by tensor copies;
+ *                                  2 target window in registers.  The fields
+ *                                  are identical for all three.
  * nli_ctx_get_tuning reads them back. */
 #define NLI_TUNE_CG_CLUSTER_CAP 0
 #define NLI_TUNE_CG_UNKNOWNS_PER_CTA 1
 #define NLI_TUNE_BATCH_WIDTH 2
+#define NLI_TUNE_PM_VARIANT 3
 int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value);
 int nli_ctx_get_tuning(nli_ctx *ctx, int knob, int *value);
 /* The seed image `index` of a batch runs with. */

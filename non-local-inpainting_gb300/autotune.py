@@ -1,11 +1,13 @@
 """Autotuner for the launch shapes the library leaves open: the size of the
 thread-block clusters of the NL-Poisson conjugate gradient (CTAs per
-cluster, unknowns per CTA) and the number of images a batch keeps in
+cluster, unknowns per CTA), the way the 9x9 PatchMatch kernels read their
+windows (NLI_TUNE_PM_VARIANT) and the number of images a batch keeps in
 flight.  Each candidate is timed with CUDA events on a representative case
 on the context's own device; the fastest is set on the context
 (nli_ctx_set_tuning) and returned with the whole table, which callers may
 store and re-apply with apply().  Results depend on these shapes only
-through the float rounding of the CG's sums.
+through the float rounding of the CG's sums; the PatchMatch variants give
+identical fields.
 """
 from __future__ import annotations
 
@@ -60,6 +62,47 @@ def tune_cg(ctx, case=None, caps=(4, 8, 12, 16), per_cta=(512, 1024, 2048), repe
     return {"best": choice, "ms": times}
 
 
+def patchmatch_case(ctx, size=512, hole=0.15, seed=0):
+    """A finest-level PatchMatch case (9x9 L2 combined, 10 sweeps): Poisson
+    filled Voronoi texture with an ellipse hole and the driver's masks."""
+    import numpy as np
+    from . import workloads as wl
+    rng = np.random.default_rng(seed)
+    img, _ = wl.voronoi_texture(size, size, 40, rng)
+    mask = wl.ellipse_mask(size, size, 6, hole, rng)
+    p = wl.params("nlpoisson", scales=2, coarse=0.5, iters=1, cg_tol=1e-4)
+    ext = ctx.extended_domain(mask, 9, 9)
+    src, tgt, _ = ctx.scale_masks(ext, 4, True)
+    u = ctx.poisson_init(img, mask)
+    return p.distance, p.patchmatch, u, src, tgt
+
+
+def tune_pm_variant(ctx, case=None, variants=(0, 1, 2), repeats=3, seed=0):
+    """Times one PatchMatch call per window variant and keeps the fastest.
+    Returns {"best": variant, "ms": {variant: ms}}."""
+    import torch
+    dist, pm, u, src, tgt = case if case is not None else patchmatch_case(ctx)
+    times = {}
+    for v in variants:
+        ctx.set_tuning(ctx.TUNE_PM_VARIANT, v)
+        ctx.set_seed(seed)
+        ctx.patchmatch(dist, pm, u, src, u, tgt, want_energy=False)  # warm
+        best = float("inf")
+        for _ in range(repeats):
+            ctx.set_seed(seed)
+            torch.cuda.synchronize()
+            a, b = _events(torch)
+            a.record()
+            ctx.patchmatch(dist, pm, u, src, u, tgt, want_energy=False)
+            b.record()
+            torch.cuda.synchronize()
+            best = min(best, a.elapsed_time(b))
+        times[v] = best
+    choice = min(times, key=times.get)
+    ctx.set_tuning(ctx.TUNE_PM_VARIANT, choice)
+    return {"best": choice, "ms": times}
+
+
 def tune_batch_width(ctx, items, params, widths=(2, 4, 8, 12, 16)):
     """Times process_batch_device on device-resident `items` per batch width
     and keeps the fastest.  Returns {"best": width, "ms": {width: ms}}."""
@@ -79,10 +122,12 @@ def tune_batch_width(ctx, items, params, widths=(2, 4, 8, 12, 16)):
     return {"best": choice, "ms": times}
 
 
-def apply(ctx, cg=None, batch_width=None):
+def apply(ctx, cg=None, batch_width=None, pm_variant=None):
     """Re-applies stored choices: cg = (cap, unknowns per CTA)."""
     if cg is not None:
         ctx.set_tuning(ctx.TUNE_CG_CLUSTER_CAP, int(cg[0]))
         ctx.set_tuning(ctx.TUNE_CG_UNKNOWNS_PER_CTA, int(cg[1]))
+    if pm_variant is not None:
+        ctx.set_tuning(ctx.TUNE_PM_VARIANT, int(pm_variant))
     if batch_width is not None:
         ctx.set_batch_width(int(batch_width))

@@ -141,6 +141,7 @@ int nli_ctx_create(int device, nli_ctx **out)
 		NLI_CUDA(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
 		ctx->stream = ctx->own_stream;
 		NLI_CUDA(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
+		NLI_CUDA(cudaDeviceGetAttribute(&ctx->max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
 		NLI_CUDA(cudaMallocHost(&ctx->host_pinned, 4096));
 		NLI_CUDA(cudaMalloc(&ctx->status, sizeof(DevStatus)));
 		NLI_CUDA(cudaMemset(ctx->status, 0, sizeof(DevStatus)));
@@ -576,6 +577,10 @@ int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value)
 		if (value < 1) return NLI_E_INVALID;
 		ctx->batch_width = value;
 		return NLI_OK;
+	case NLI_TUNE_PM_VARIANT:
+		if (value < 0 || value > 2) return NLI_E_INVALID;
+		ctx->tune_pm_variant = value;
+		return NLI_OK;
 	}
 	return NLI_E_INVALID;
 }
@@ -587,6 +592,7 @@ int nli_ctx_get_tuning(nli_ctx *ctx, int knob, int *value)
 	case NLI_TUNE_CG_CLUSTER_CAP: *value = ctx->tune_cg_cluster_cap; return NLI_OK;
 	case NLI_TUNE_CG_UNKNOWNS_PER_CTA: *value = ctx->tune_cg_unknowns_per_cta; return NLI_OK;
 	case NLI_TUNE_BATCH_WIDTH: *value = ctx->batch_width; return NLI_OK;
+	case NLI_TUNE_PM_VARIANT: *value = ctx->tune_pm_variant; return NLI_OK;
 	}
 	return NLI_E_INVALID;
 }

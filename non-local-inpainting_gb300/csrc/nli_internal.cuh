@@ -120,6 +120,8 @@ struct nli_ctx {
 	// tunable launch shapes (nli_ctx_set_tuning)
 	int tune_cg_cluster_cap = 16;        // CTAs per CG cluster at most
 	int tune_cg_unknowns_per_cta = 1024; // at least this many unknowns per CG CTA
+	int tune_pm_variant = 0;             // 9x9 PatchMatch window reads (PmVariant)
+	int max_smem_optin = 0;              // dynamic shared memory per block at most
 	std::vector<nli_ctx *> workers;
 	std::vector<cudaEvent_t> event_pool;
 

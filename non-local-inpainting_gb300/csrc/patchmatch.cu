@@ -34,11 +34,91 @@
 // step (propagation, then random search) are gathered first, one per lane,
 // then evaluated K at a time and accepted in their sequential order with a
 // strict "<", so the result equals evaluating them one after the other.
+#include <cuda.h>  // CUtensorMap (the descriptor type; encoded through the runtime's driver entry point)
+
 #include "nli_device.cuh"
 
 namespace nli {
 
 constexpr unsigned kFull = 0xffffffffu;
+
+// ------------------------------------------------------- TMA staging
+// With 9 x 9 patches each candidate's source window (rows x L float4) is
+// copied into the warp's shared memory by one tensor copy
+// (cp.async.bulk.tensor.2d) instead of being read row by row through L1.
+// The copies of a step complete on the warp's mbarrier; waiting is bounded
+// and a wait that runs out sets the context's timeout flag.
+constexpr unsigned kTmaWaitLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
+{
+	asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+	asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes)
+{
+	asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity)
+{
+	uint32_t ok;
+	asm volatile(
+	    "{\n\t.reg .pred p;\n\t"
+	    "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+	    "selp.u32 %0, 1, 0, p;\n\t}"
+	    : "=r"(ok)
+	    : "r"(smem_u32(bar)), "r"(parity)
+	    : "memory");
+	return ok != 0;
+}
+
+// Bounded wait for the phase `parity` of the barrier; false when it ran out.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
+{
+	for (unsigned i = 0; i < kTmaWaitLimit; i++)
+		if (mbar_try_wait(bar, parity)) return true;
+	return false;
+}
+
+// Orders this thread's earlier generic-proxy accesses of shared memory
+// before later async-proxy (tensor copy) writes to it.
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Tile [x, x + box0) x [y, y + box1) of the 2-D tensor into dst; x counts
+// floats and is a multiple of 4 (16 bytes) here.
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar)
+{
+	asm volatile(
+	    "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+	        smem_u32(dst)),
+	    "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+	    : "memory");
+}
+
+// How the fixed-size (9 x 9) kernels read a candidate's two windows
+// (NLI_TUNE_PM_VARIANT): kPmShared keeps the target window in shared memory
+// and loads source rows from global memory (32 warps per SM); kPmStaged also
+// copies the source windows into shared memory by tensor copies; kPmRegs
+// holds the lane's column of the target window in registers (16 warps per
+// SM, twice the registers).  All three evaluate the same candidates with the
+// same arithmetic.  Runtime-sized patches always use kPmShared.
+enum PmVariant { kPmShared = 0, kPmStaged = 1, kPmRegs = 2 };
+
+__host__ __device__ constexpr int pm_threads(int V) { return V == kPmRegs ? 512 : 1024; }
+
+// Per-warp state of the staged path.
+struct TmaState {
+	const CUtensorMap *map;
+	float4 *slots;    // K windows of rows x L float4, each slot_stride float4 apart
+	int slot_stride;  // float4
+	uint64_t *bar;
+	unsigned phase;
+	int *timeout;  // context status flag
+};
 
 struct PmArgs {
 	const float4 *src;  // source pixels, (sW + 1) x (sH + 1), row stride sWp
@@ -114,6 +194,23 @@ __device__ __forceinline__ void load_window(const PmArgs &p, const float *s_w, i
 		s_t[e] = v;
 	}
 	__syncwarp();
+}
+
+// kPmRegs: the lane's column c of the same window, tw[r] = element r * L + c
+// of load_window's, for a fixed P x P patch.
+template <int KIND, int C, int P>
+__device__ __forceinline__ void load_window_regs(const PmArgs &p, const float *s_w, int x, int y, float4 *tw)
+{
+	constexpr int L = P + (Kind<KIND>::grad ? 1 : 0);
+	const int lane = threadIdx.x & 31;
+	const int c = lane - (lane / L) * L;
+	const float4 *T = p.tgt + (size_t)(y - p.ry) * p.tWp + (x - p.rx) + c;
+#pragma unroll
+	for (int r = 0; r < L; r++) {
+		float4 v = __ldg(T + (size_t)r * p.tWp);
+		if (C <= 3) v.w = (r < P && c < P) ? s_w[r * P + c] : 0.f;
+		tw[r] = v;
+	}
 }
 
 template <int C>
@@ -239,12 +336,18 @@ __device__ __forceinline__ float combine(const Acc &A, const PmArgs &p)
 // current distance for every candidate of a step, the rest of the step is
 // skipped (exact: all terms are non-negative).  P > 0: square P x P patch
 // known at compile time (rows unrolled); P == 0: sizes from the arguments.
-template <int KIND, int C, int P>
+// kPmStaged: the step's source windows are copied into the warp's slots
+// first (one tensor copy per candidate) and the rows are read from there.
+// kPmRegs: the target rows come from tw (registers) instead of s_t.
+template <int KIND, int C, int P, int V = kPmShared>
 __device__ __forceinline__ void eval_candidates(const PmArgs &p, const float *s_w, const float4 *s_t, int mycand,
-                                                int n, int2 &best, float &bd, unsigned &partial)
+                                                int n, int2 &best, float &bd, unsigned &partial,
+                                                TmaState *ts = nullptr, const float4 *tw = nullptr)
 {
+	constexpr bool TMA = V == kPmStaged;
 	constexpr bool G = Kind<KIND>::grad;
 	constexpr int PF = (C == 4) ? 1 : 2;  // rows of loads in flight (fewer for 4 channels: registers)
+	if (TMA && ts->map == nullptr) return;  // this warp's staging gave up (timeout flagged)
 	const int L = P ? P + G : p.L;
 	const int K = P ? 32 / (P + G) : p.K;
 	const int rows = P ? P + G : p.rows;
@@ -266,22 +369,58 @@ __device__ __forceinline__ void eval_candidates(const PmArgs &p, const float *s_
 		const float4 *S = p.src + (size_t)(cy - p.ry) * sWp + (cx - p.rx) + c;
 		const float4 *T = s_t + c;
 		const float *Wt = s_w + c;
-		float4 v0 = active ? __ldg(S) : zero;
-		float4 v1 = (PF == 2 && active && rows > 1) ? __ldg(S + sWp) : zero;
+		const float4 *Sl = nullptr;  // this lane's column of its candidate's staged window
+		if constexpr (TMA) {
+			static_assert(P > 0, "the staged path is compiled for fixed patch sizes");
+			constexpr int KC = 32 / (P + G);
+			const int nact = min(K, n - b);
+			int cs[KC];
+#pragma unroll
+			for (int s = 0; s < KC; s++) cs[s] = __shfl_sync(kFull, mycand, min(b + s, 31));
+			__syncwarp();
+			if (lane == 0) {
+				fence_proxy_async();
+				mbar_expect_tx(ts->bar, (unsigned)(nact * rows * L * sizeof(float4)));
+#pragma unroll
+				for (int s = 0; s < KC; s++)
+					if (s < nact)
+						tma_load_2d(ts->slots + s * ts->slot_stride, ts->map, 4 * ((cs[s] & 0xffff) - p.rx),
+						            (cs[s] >> 16) - p.ry, ts->bar);
+			}
+			const bool landed = __all_sync(kFull, mbar_wait(ts->bar, ts->phase));
+			if (!landed) {
+				// the copies did not land in time: flag it, give them one more
+				// bounded wait, and stop using this warp's slots
+				if (lane == 0) atomicExch(ts->timeout, 1);
+				mbar_wait(ts->bar, ts->phase);
+				ts->map = nullptr;
+				return;
+			}
+			ts->phase ^= 1u;
+			Sl = ts->slots + (active ? sw : 0) * ts->slot_stride + c;
+		}
+		float4 v0 = (!TMA && active) ? __ldg(S) : zero;
+		float4 v1 = (!TMA && PF == 2 && active && rows > 1) ? __ldg(S + sWp) : zero;
 		float4 dp = zero;
 		float wp = 0.f;
 		Acc A = {0.f, 0.f, 0.f, 0.f};
 		const float bound = bd;
 		bool stop = false;
 		auto row = [&](int r) {
-			const float4 v = v0;
-			if (PF == 2) {
+			float4 v = v0;
+			if (TMA) {
+				v = active ? Sl[r * L] : zero;
+			} else if (PF == 2) {
 				v0 = v1;
 				v1 = (active && r + 2 < rows) ? __ldg(S + (size_t)(r + 2) * sWp) : zero;
 			} else {
 				v0 = (active && r + 1 < rows) ? __ldg(S + (size_t)(r + 1) * sWp) : zero;
 			}
-			const float4 t = T[r * L];
+			float4 t;
+			if constexpr (V == kPmRegs)
+				t = tw[r];
+			else
+				t = T[r * L];
 			const float4 d = subc<C>(v, t);
 			const bool tap = act_col && r < py;
 			const float w = (C <= 3) ? t.w : (tap ? Wt[r * px] : 0.f);
@@ -356,27 +495,65 @@ struct PmSmem {
 	float *w;
 	float4 *t;
 	int *list;
+	float4 *slots;  // staged path: K windows per warp
+	int slot_stride;
+	uint64_t *bar;
 };
 
+// Staged path layout (float4 units, from a 128-byte aligned base): the
+// weights, then per warp a region of the target window, K window slots, the
+// candidate list and the mbarrier, every part starting on 128 bytes.
+__host__ __device__ inline int pm_round8(int v) { return (v + 7) & ~7; }
+
+__host__ __device__ inline int pm_tma_region(int rows, int L, int K)
+{
+	return pm_round8(pm_round8(rows * L) * (1 + K) + 8 + 1);
+}
+
+__host__ __device__ inline size_t pm_smem_bytes_tma(int taps, int rows, int L, int K, int warps)
+{
+	return 128 + sizeof(float4) * ((size_t)pm_round8(pm_weight_slots(taps)) + (size_t)warps * pm_tma_region(rows, L, K));
+}
+
+template <int V>
 __device__ __forceinline__ PmSmem pm_smem(const DistArgs &a, const PmArgs &p)
 {
 	extern __shared__ float4 s_pm[];
 	const int warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
 	PmSmem m;
 	const int ws = pm_weight_slots(a.px * a.py);
-	m.w = reinterpret_cast<float *>(s_pm);
-	m.t = s_pm + ws + warp * p.rows * p.L;
-	m.list = reinterpret_cast<int *>(s_pm + ws + warps * p.rows * p.L) + warp * 32;
+	if (V != kPmStaged) {
+		m.w = reinterpret_cast<float *>(s_pm);
+		m.t = s_pm + ws + warp * p.rows * p.L;
+		m.list = reinterpret_cast<int *>(s_pm + ws + warps * p.rows * p.L) + warp * 32;
+		m.slots = nullptr;
+		m.slot_stride = 0;
+		m.bar = nullptr;
+	} else {
+		float4 *base = reinterpret_cast<float4 *>((reinterpret_cast<uintptr_t>(s_pm) + 127) & ~(uintptr_t)127);
+		const int win = pm_round8(p.rows * p.L);
+		float4 *r = base + pm_round8(ws) + (size_t)warp * pm_tma_region(p.rows, p.L, p.K);
+		m.w = reinterpret_cast<float *>(base);
+		m.t = r;
+		m.slots = r + win;
+		m.slot_stride = win;
+		m.list = reinterpret_cast<int *>(r + win * (1 + p.K));
+		m.bar = reinterpret_cast<uint64_t *>(r + win * (1 + p.K) + 8);
+	}
 	return m;
 }
 
-template <int KIND, int C, int P>
-__global__ void __launch_bounds__(1024, 1) k_pm_init(DistArgs a, PmArgs p, const int2 *__restrict__ init,
+template <int KIND, int C, int P, int V>
+__global__ void __launch_bounds__(pm_threads(V), 1) k_pm_init(DistArgs a, PmArgs p, const int2 *__restrict__ init,
                                                       int2 *__restrict__ nnf, float *__restrict__ dist,
-                                                      unsigned long long *counter)
+                                                      unsigned long long *counter,
+                                                      const __grid_constant__ CUtensorMap tmap, int *timeout)
 {
 	const int lane = threadIdx.x & 31;
-	const PmSmem m = pm_smem(a, p);
+	const PmSmem m = pm_smem<V>(a, p);
+	TmaState ts = {&tmap, m.slots, m.slot_stride, m.bar, 0u, timeout};
+	if (V == kPmStaged && lane == 0) mbar_init(m.bar, 1);
+	float4 tw[(V == kPmRegs) ? P + 1 : 1];
 	load_weights(a, m.w);
 	unsigned evals = 0, partial = 0;
 	// block b takes the contiguous range [b * chunk, (b + 1) * chunk) of the
@@ -409,8 +586,11 @@ __global__ void __launch_bounds__(1024, 1) k_pm_init(DistArgs a, PmArgs p, const
 		float d = FLT_MAX;
 		int2 best = make_int2(-1, -1);
 		if (src_ok(p, n.x, n.y) && tgt_patch_inside(p, x, y)) {
-			load_window<C>(p, m.w, x, y, m.t);
-			eval_candidates<KIND, C, P>(p, m.w, m.t, n.x | (n.y << 16), 1, best, d, partial);
+			if constexpr (V == kPmRegs)
+				load_window_regs<KIND, C, P>(p, m.w, x, y, tw);
+			else
+				load_window<C>(p, m.w, x, y, m.t);
+			eval_candidates<KIND, C, P, V>(p, m.w, m.t, n.x | (n.y << 16), 1, best, d, partial, &ts, tw);
 			evals++;
 			__syncwarp();
 		}
@@ -428,15 +608,19 @@ __global__ void __launch_bounds__(1024, 1) k_pm_init(DistArgs a, PmArgs p, const
 // metric_prop (may be NULL): this sweep's count of target points that the
 // propagation step improved; metric_shots (may be NULL): the largest index
 // of a first accepted random draw (patch_match.cpp:452-456, 481-485).
-template <int KIND, int C, int P>
-__global__ void __launch_bounds__(1024, 1) k_pm_sweep(DistArgs a, PmArgs p, int sweep, int jump,
+template <int KIND, int C, int P, int V>
+__global__ void __launch_bounds__(pm_threads(V), 1) k_pm_sweep(DistArgs a, PmArgs p, int sweep, int jump,
                                                        const int2 *__restrict__ nnf_in, const float *__restrict__ dist_in,
                                                        int2 *__restrict__ nnf_out, float *__restrict__ dist_out,
                                                        unsigned long long *counter, unsigned long long *metric_prop,
-                                                       int *metric_shots)
+                                                       int *metric_shots, const __grid_constant__ CUtensorMap tmap,
+                                                       int *timeout)
 {
 	const int lane = threadIdx.x & 31;
-	const PmSmem m = pm_smem(a, p);
+	const PmSmem m = pm_smem<V>(a, p);
+	TmaState ts = {&tmap, m.slots, m.slot_stride, m.bar, 0u, timeout};
+	if (V == kPmStaged && lane == 0) mbar_init(m.bar, 1);
+	float4 tw[(V == kPmRegs) ? P + 1 : 1];
 	load_weights(a, m.w);
 	unsigned evals = 0, partial = 0, improved = 0;
 	int max_shot = -1;
@@ -450,7 +634,10 @@ __global__ void __launch_bounds__(1024, 1) k_pm_sweep(DistArgs a, PmArgs p, int 
 		int2 best = nnf_in[pix];
 		float bd = dist_in[pix];
 		if (tgt_patch_inside(p, x, y)) {
-			load_window<C>(p, m.w, x, y, m.t);
+			if constexpr (V == kPmRegs)
+				load_window_regs<KIND, C, P>(p, m.w, x, y, tw);
+			else
+				load_window<C>(p, m.w, x, y, m.t);
 			// propagation: lane 4s + k proposes the match of neighbour k
 			// (left, right, up, down) at distance 1 (s = 0) or at the jump
 			// distance (s = 1), shifted back by the neighbour's offset
@@ -473,7 +660,7 @@ __global__ void __launch_bounds__(1024, 1) k_pm_sweep(DistArgs a, PmArgs p, int 
 			int n = compact_candidates(valid, packed, best, m.list, mycand);
 			evals += n;
 			const float bd_before = bd;
-			eval_candidates<KIND, C, P>(p, m.w, m.t, mycand, n, best, bd, partial);
+			eval_candidates<KIND, C, P, V>(p, m.w, m.t, mycand, n, best, bd, partial, &ts, tw);
 			if (bd < bd_before) improved++;
 			// random search around the match after propagation: lane k draws
 			// in window max_window >> k from its own stream, up to `shots`
@@ -498,7 +685,7 @@ __global__ void __launch_bounds__(1024, 1) k_pm_sweep(DistArgs a, PmArgs p, int 
 			}
 			n = compact_candidates(valid, packed, best, m.list, mycand);
 			evals += n;
-			eval_candidates<KIND, C, P>(p, m.w, m.t, mycand, n, best, bd, partial);
+			eval_candidates<KIND, C, P, V>(p, m.w, m.t, mycand, n, best, bd, partial, &ts, tw);
 			__syncwarp();
 		} else {
 			best = make_int2(-1, -1);
@@ -573,31 +760,100 @@ struct PmMetrics {
 
 static void sweep_energy(cudaStream_t s, const PmArgs &p, const float *dist, const PmMetrics &m, int sweep);
 
-template <int KIND, int C, int P>
-static void run_sweeps(nli_ctx *ctx, const DistArgs &a, const PmArgs &p, int iterations, const int2 *init,
-                       int2 *nnf_x, float *dist_x, int2 *nnf_y, float *dist_y, unsigned long long *counter,
-                       const PmMetrics &mt)
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no
+// link against the driver library); null when the driver does not have it.
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled()
 {
-	// persistent: one 32-warp block per SM (fewer when there are fewer points)
-	const int block = 1024;
+	static const EncodeTiledFn fn = [] {
+		void *f = nullptr;
+		cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+		if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+		        cudaSuccess ||
+		    q != cudaDriverEntryPointSuccess) {
+			(void)cudaGetLastError();
+			return static_cast<EncodeTiledFn>(nullptr);
+		}
+		return reinterpret_cast<EncodeTiledFn>(f);
+	}();
+	return fn;
+}
+
+// The padded source as a 2-D float tensor (4 * sWp floats by sH + 1 rows)
+// with a box of one candidate window (4 * L floats by rows).  False when it
+// cannot be encoded; the caller then reads the windows with plain loads.
+static bool encode_source_map(const PmArgs &p, CUtensorMap *map)
+{
+	const EncodeTiledFn enc = encode_tiled();
+	if (!enc) return false;
+	if ((reinterpret_cast<uintptr_t>(p.src) & 15) != 0 || 4 * p.L > 256 || p.rows > 256) return false;
+	const cuuint64_t dim[2] = {(cuuint64_t)4 * p.sWp, (cuuint64_t)p.sH + 1};
+	const cuuint64_t stride[1] = {(cuuint64_t)p.sWp * sizeof(float4)};
+	const cuuint32_t box[2] = {(cuuint32_t)(4 * p.L), (cuuint32_t)p.rows};
+	const cuuint32_t estride[2] = {1, 1};
+	return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float4 *>(p.src), dim, stride, box, estride,
+	           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+	           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int KIND, int C, int P, int V>
+static void launch_sweeps(nli_ctx *ctx, const DistArgs &a, const PmArgs &p, int iterations, const int2 *init,
+                          int2 *nnf_x, float *dist_x, int2 *nnf_y, float *dist_y, unsigned long long *counter,
+                          const PmMetrics &mt, const CUtensorMap &map, size_t smem)
+{
+	// persistent: one block per SM (fewer when there are fewer points)
+	const int block = pm_threads(V);
 	const int grid = (int)std::min<size_t>(((size_t)p.nt * 32 + block - 1) / block, (size_t)ctx->num_sms);
-	const size_t smem = pm_smem_bytes(a.px * a.py, p.rows, p.L, block / 32);
-	NLI_CUDA(cudaFuncSetAttribute(k_pm_init<KIND, C, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-	NLI_CUDA(cudaFuncSetAttribute(k_pm_sweep<KIND, C, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	int *timeout = &ctx->status->timeout;
+	NLI_CUDA(cudaFuncSetAttribute(k_pm_init<KIND, C, P, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	NLI_CUDA(cudaFuncSetAttribute(k_pm_sweep<KIND, C, P, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 	{
 		ProfScope ps(ctx, "pm_init");
-		k_pm_init<KIND, C, P><<<grid, block, smem, ctx->stream>>>(a, p, init, nnf_x, dist_x, counter);
+		k_pm_init<KIND, C, P, V><<<grid, block, smem, ctx->stream>>>(a, p, init, nnf_x, dist_x, counter, map,
+		                                                                timeout);
 		NLI_CHECK_LAUNCH();
 	}
 	for (int it = 0; it < iterations; it++) {
 		const bool even = (it % 2) == 0;
 		ProfScope ps(ctx, "pm_sweep");
-		k_pm_sweep<KIND, C, P><<<grid, block, smem, ctx->stream>>>(
+		k_pm_sweep<KIND, C, P, V><<<grid, block, smem, ctx->stream>>>(
 		    a, p, it, jump_for(it, p.tW, p.tH), even ? nnf_x : nnf_y, even ? dist_x : dist_y, even ? nnf_y : nnf_x,
-		    even ? dist_y : dist_x, counter, mt.prop ? mt.prop + it : nullptr, mt.shots);
+		    even ? dist_y : dist_x, counter, mt.prop ? mt.prop + it : nullptr, mt.shots, map, timeout);
 		NLI_CHECK_LAUNCH();
 		if (mt.energy) sweep_energy(ctx->stream, p, even ? dist_y : dist_x, mt, it);
 	}
+}
+
+// Fixed-size patches take the context's variant; the staged one only when
+// the tensor map encodes and its layout fits, else (and for runtime-sized
+// patches) kPmShared.
+template <int KIND, int C, int P>
+static void run_sweeps(nli_ctx *ctx, const DistArgs &a, const PmArgs &p, int iterations, const int2 *init,
+                       int2 *nnf_x, float *dist_x, int2 *nnf_y, float *dist_y, unsigned long long *counter,
+                       const PmMetrics &mt)
+{
+	const int taps = a.px * a.py;
+	CUtensorMap map;
+	std::memset(&map, 0, sizeof(map));
+	if constexpr (P > 0) {
+		if (ctx->tune_pm_variant == kPmStaged) {
+			const size_t smem = pm_smem_bytes_tma(taps, p.rows, p.L, p.K, pm_threads(kPmStaged) / 32);
+			if (smem <= (size_t)ctx->max_smem_optin && encode_source_map(p, &map)) {
+				launch_sweeps<KIND, C, P, kPmStaged>(ctx, a, p, iterations, init, nnf_x, dist_x, nnf_y, dist_y,
+				                                     counter, mt, map, smem);
+				return;
+			}
+		} else if (ctx->tune_pm_variant == kPmRegs) {
+			launch_sweeps<KIND, C, P, kPmRegs>(ctx, a, p, iterations, init, nnf_x, dist_x, nnf_y, dist_y, counter,
+			                                   mt, map, pm_smem_bytes(taps, p.rows, p.L, pm_threads(kPmRegs) / 32));
+			return;
+		}
+	}
+	launch_sweeps<KIND, C, P, kPmShared>(ctx, a, p, iterations, init, nnf_x, dist_x, nnf_y, dist_y, counter, mt, map,
+	                                     pm_smem_bytes(taps, p.rows, p.L, pm_threads(kPmShared) / 32));
 }
 
 static void sweep_energy(cudaStream_t s, const PmArgs &p, const float *dist, const PmMetrics &m, int sweep)
@@ -729,7 +985,10 @@ void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patch
 			unsigned long long *hc = reinterpret_cast<unsigned long long *>(ctx->host_pinned);
 			NLI_CUDA(cudaMemcpyAsync(hc, counter, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
 			NLI_CUDA(cudaMemcpyAsync(hc + 2, partials + eg, sizeof(double), cudaMemcpyDeviceToHost, s));
+			NLI_CUDA(cudaMemcpyAsync(hc + 3, &ctx->status->timeout, sizeof(int), cudaMemcpyDeviceToHost, s));
 			NLI_CUDA(cudaStreamSynchronize(s));
+			NLI_REQUIRE(*reinterpret_cast<const int *>(hc + 3) == 0, NLI_E_TIMEOUT,
+			            "PatchMatch window copies timed out");
 			ctx->candidates += (int64_t)hc[0];
 			ctx->candidates_partial += (int64_t)hc[1];
 			*energy = *reinterpret_cast<double *>(hc + 2);

@@ -905,7 +905,11 @@ static double read_total(nli_ctx *ctx, double *partials, int n, int *cg_iters_de
 	NLI_CUDA(cudaMemcpyAsync(h, partials + n, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
 	if (cg_iters_dev)
 		NLI_CUDA(cudaMemcpyAsync(h + 64, cg_iters_dev, sizeof(int) * 4, cudaMemcpyDeviceToHost, ctx->stream));
+	// timeouts of the waits of this iteration's kernels (PatchMatch's tensor
+	// copies, CG grid barriers)
+	NLI_CUDA(cudaMemcpyAsync(h + 128, &ctx->status->timeout, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
 	NLI_CUDA(cudaStreamSynchronize(ctx->stream));
+	NLI_REQUIRE(*reinterpret_cast<const int *>(h + 128) == 0, NLI_E_TIMEOUT, "a device-side wait timed out");
 	if (cg_iters_dev) {
 		const int *it = reinterpret_cast<const int *>(h + 64);
 		for (int c = 0; c < C; c++) {
@@ -1107,11 +1111,7 @@ double update_run(nli_ctx *ctx, const nli_update_params &up, float *image, const
 			launch_sum_partials(s, diff_part, np, diff_part + np);
 			return 0.0;
 		}
-		const double t = read_total(ctx, diff_part, np, ctx->buf<int>("poi.iters", 4), C, nh);
-		int *hs = static_cast<int *>(ctx->host_pinned) + 128;
-		NLI_CUDA(cudaMemcpy(hs, &ctx->status->timeout, sizeof(int), cudaMemcpyDeviceToHost));
-		NLI_REQUIRE(*hs == 0, NLI_E_TIMEOUT, "conjugate gradient grid barrier timed out");
-		return t;
+		return read_total(ctx, diff_part, np, ctx->buf<int>("poi.iters", 4), C, nh);
 	}
 	float *newval = ctx->buf<float>("upd.newval", (size_t)nh * C);
 	int grid;

@@ -26,6 +26,16 @@ def test_tune_cg(gpu_ctx):
     autotune.apply(gpu_ctx, cg=(16, 1024))  # back to the defaults for later tests
 
 
+def test_tune_pm_variant(gpu_ctx):
+    from nli_gb300 import autotune
+    case = autotune.patchmatch_case(gpu_ctx, size=160, seed=2)
+    res = autotune.tune_pm_variant(gpu_ctx, case, repeats=1)
+    assert sorted(res["ms"]) == [0, 1, 2] and res["best"] in res["ms"]
+    assert gpu_ctx.get_tuning(gpu_ctx.TUNE_PM_VARIANT) == res["best"]
+    autotune.apply(gpu_ctx, pm_variant=0)
+    assert gpu_ctx.get_tuning(gpu_ctx.TUNE_PM_VARIANT) == 0
+
+
 def test_tuning_knobs_validate(gpu_ctx):
     from nli_gb300 import NliError
     with pytest.raises(NliError):
