@@ -435,9 +435,10 @@ def batch_compare(pkg, ctx, args, local):
 
 
 def run_case(args):
-    """Small single-kernel cases for profiler captures: one PatchMatch call
-    (init + 10 sweeps) or one NL-Poisson update on the finest scale of the
-    benchmark workload, with the masks the driver builds there."""
+    """Cases for profiler captures: one PatchMatch call (init + 10 sweeps) or
+    one NL-Poisson update on the finest scale of the benchmark workload, with
+    the masks the driver builds there; or whole process() calls (`process`,
+    the launch sequence of one benchmark step per --steps)."""
     import torch
     pkg = ge.package()
     ctx = pkg.Context(0)
@@ -445,6 +446,16 @@ def run_case(args):
         ctx.set_tuning(ctx.TUNE_PM_VARIANT, args.pm_variant)
     ctx.set_seed(7)
     img, mask, p = workload()
+    if args.case == "process":
+        d_img, d_mask = ctx._f32(img), ctx._u8(mask)
+        d_out = torch.empty_like(d_img)
+        l0 = ctx.launch_count()
+        for _ in range(args.steps):
+            ctx.set_seed(1234)
+            _, st = ctx.process_device(d_img, d_mask, p, out=d_out)
+        torch.cuda.synchronize()
+        print(json.dumps({"case": "process", "launches": ctx.launch_count() - l0, "stats": st}))
+        return 0
     ext = ctx.extended_domain(mask, p.update.patch_x, p.update.patch_y)
     src, tgt, _ = ctx.scale_masks(ext, p.update.patch_x // 2, True)
     d_img = ctx._f32(img)
@@ -463,7 +474,7 @@ def run_case(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default=None, choices=["patchmatch", "update"],
+    ap.add_argument("--case", default=None, choices=["patchmatch", "update", "process"],
                     help="run one small profiling case instead of the benchmark")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
