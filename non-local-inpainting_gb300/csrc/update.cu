@@ -632,7 +632,9 @@ __global__ void __launch_bounds__(kCgBlock) k_poisson_cg(PoissonArgs a, const Un
 // Two cluster barriers per iteration; block partial sums are exchanged
 // through distributed shared memory and added in rank order by one warp,
 // so every CTA holds the same totals.  alpha and beta are formed once per
-// CTA in double precision.
+// CTA in double precision by that warp and published with one block
+// barrier.  (Pushing the partials into every CTA before the barrier, so
+// that the totals are read locally, measured no faster.)
 constexpr int kClusterBlock = 512;
 constexpr int kClusterMax = 16;
 constexpr int kClusterMaxChunk = 4096;
@@ -679,6 +681,7 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 	__shared__ double partA[4], partB[4], tot[4];
 	__shared__ float s_coef[4];
 	__shared__ int s_active[4];
+	__shared__ double s_nr[4];
 	__shared__ float *base[3][kClusterMax];  // r, dA, dB of every CTA
 	const int rank = (int)cluster.block_rank(), ncta = (int)cluster.num_blocks();
 	const int group = (int)blockIdx.x / ncta, cb = group * C;  // this cluster's first channel
@@ -698,6 +701,8 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 	for (int l = threadIdx.x; l < own; l += blockDim.x) s_unk[l] = unk_g[lo + l];
 	__syncthreads();
 
+	// block partial sums per channel into dst (written by warp 0; read by
+	// the other CTAs after the next cluster barrier)
 	auto block_reduce = [&](const float *v, double *dst) {
 #pragma unroll
 		for (int c = 0; c < C; c++) {
@@ -705,25 +710,22 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 			if (lane == 0) red[wid][c] = (double)s;
 		}
 		__syncthreads();
-		if (threadIdx.x < C) {
-			double s = 0.0;
-			for (int w = 0; w < kClusterBlock / 32; w++) s += red[w][threadIdx.x];
-			dst[threadIdx.x] = s;
-		}
-	};
-	auto cluster_total = [&](double *src, double *out) {
 		if (wid == 0) {
 #pragma unroll
 			for (int c = 0; c < C; c++) {
-				double v = (lane < ncta) ? cluster.map_shared_rank(src, lane)[c] : 0.0;
-				v = warp_sum(v);
-				if (lane == 0) tot[c] = v;
+				const double s = warp_sum((lane < kClusterBlock / 32) ? red[lane][c] : 0.0);
+				if (lane == 0) dst[c] = s;
 			}
 		}
-		__syncthreads();
+	};
+	// cluster totals of the block partials src, in rank order, left in every
+	// lane of warp 0 (call from warp 0 only, after a cluster barrier)
+	auto warp0_totals = [&](const double *src, double *out) {
 #pragma unroll
-		for (int c = 0; c < C; c++) out[c] = tot[c];
-		__syncthreads();
+		for (int c = 0; c < C; c++) {
+			const double v = warp_sum((lane < ncta) ? cluster.map_shared_rank(const_cast<double *>(src), lane)[c] : 0.0);
+			out[c] = __shfl_sync(0xffffffffu, v, 0);
+		}
 	};
 	// channel values of vector `v` (0: r, 1: dA, 2: dB) at a 16-bit code
 	auto nb = [&](int v, uint32_t code) -> const float * {
@@ -764,7 +766,15 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 	block_reduce(facc, partB);
 	cluster.sync();
 	double nr0[4], nr[4];
-	cluster_total(partB, nr0);
+	if (wid == 0) {
+		double t[4];
+		warp0_totals(partB, t);
+		if (lane == 0)
+			for (int c = 0; c < C; c++) tot[c] = t[c];
+	}
+	__syncthreads();
+#pragma unroll
+	for (int c = 0; c < C; c++) nr0[c] = tot[c];
 	bool active[4];
 	int it[4];
 	float beta[4];
@@ -818,9 +828,13 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 		}
 		block_reduce(facc, partA);
 		cluster.sync();
-		double rq[4];
-		cluster_total(partA, rq);
-		if (threadIdx.x < C) s_coef[threadIdx.x] = active[threadIdx.x] ? (float)(nr[threadIdx.x] / rq[threadIdx.x]) : 0.f;
+		if (wid == 0) {
+			double rq[4];
+			warp0_totals(partA, rq);
+#pragma unroll
+			for (int c = 0; c < C; c++)
+				if (lane == c) s_coef[c] = active[c] ? (float)(nr[c] / rq[c]) : 0.f;
+		}
 		__syncthreads();
 		float alpha[4];
 #pragma unroll
@@ -842,29 +856,32 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 				facc[c] = fmaf(rv, rv, facc[c]);
 			}
 		}
-		// partA / partB are rewritten only after the next barrier, by which
-		// time every CTA has read them
+		// partA / partB are rewritten only after the next cluster barrier,
+		// by which time every CTA has read them
 		block_reduce(facc, partB);
 		cluster.sync();
-		double nrn[4];
-		cluster_total(partB, nrn);
-		if (threadIdx.x < C) {
-			const int c = threadIdx.x;
-			if (active[c]) {
-				s_coef[c] = (float)(nrn[c] / nr[c]);
-				s_active[c] = ((nrn[c] < (double)a.tol * nr0[c]) || (it[c] >= a.limit)) ? 0 : 1;
-			}
+		if (wid == 0) {
+			double nrn[4];
+			warp0_totals(partB, nrn);
+#pragma unroll
+			for (int c = 0; c < C; c++)
+				if (lane == c && active[c]) {
+					s_coef[c] = (float)(nrn[c] / nr[c]);
+					s_nr[c] = nrn[c];
+					s_active[c] = ((nrn[c] < (double)a.tol * nr0[c]) || (it[c] >= a.limit)) ? 0 : 1;
+				}
 		}
 		__syncthreads();
+		// s_coef, s_nr and s_active are rewritten by warp 0 only after the
+		// next block barrier, by which time every thread has read them
 #pragma unroll
 		for (int c = 0; c < C; c++) {
 			if (!active[c]) continue;
 			beta[c] = s_coef[c];
-			nr[c] = nrn[c];
+			nr[c] = s_nr[c];
 			it[c]++;
 			active[c] = s_active[c] != 0;
 		}
-		__syncthreads();
 		h = 1 - h;
 	}
 	if (rank == 0 && threadIdx.x < C) iters_out[cb + threadIdx.x] = it[threadIdx.x];
