@@ -228,6 +228,8 @@ def run_ours(args):
     ctx = pkg.Context(local)
     if args.pm_variant is not None:
         ctx.set_tuning(ctx.TUNE_PM_VARIANT, args.pm_variant)
+    if args.cg_precond is not None:
+        ctx.set_tuning(ctx.TUNE_CG_PRECOND, args.cg_precond)
     img, mask, p = workload()
     H, W, C = img.shape
     mpix = W * H / 1e6
@@ -298,6 +300,24 @@ def run_ours(args):
     e_total = max_over_ranks(sum(ems), dev)
     e2e_value = job_throughput(world, args.steps, mpix, e_total)
 
+    # the same steps with the Jacobi-preconditioned CG (NLI_TUNE_CG_PRECOND = 1):
+    # the plain CG's stopping test on the true residual, fewer iterations, a
+    # solution that differs from the reference's within the CG tolerance
+    jacobi = None
+    if world == 1 and args.cg_precond is None and not args.no_variants:
+        ctx.set_tuning(ctx.TUNE_CG_PRECOND, 1)
+        try:
+            step()
+            torch.cuda.synchronize()
+            k0 = ctx.counters()["cg_iterations"]
+            jms = timed(step, args.steps)
+            k1 = ctx.counters()["cg_iterations"]
+        finally:
+            ctx.set_tuning(ctx.TUNE_CG_PRECOND, 0)
+        jacobi = {"value": job_throughput(world, args.steps, mpix, sum(jms)), "unit": UNIT,
+                  "ms_per_step": sum(jms) / args.steps, "cg_iterations_per_step": (k1 - k0) / args.steps,
+                  "path": "plain process(), inputs resident, Jacobi-preconditioned CG"}
+
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -362,6 +382,7 @@ def run_ours(args):
         "batched": batch,
         "process_stats": {"iterations": list(st.iterations[:p.scales]), "patchmatch_calls": st.patchmatch_calls,
                           "update_calls": st.update_calls, "cg_iterations": st.cg_iterations},
+        "cg_jacobi": jacobi,
     }
     print(json.dumps(line))
     if world > 1:
@@ -444,6 +465,8 @@ def run_case(args):
     ctx = pkg.Context(0)
     if args.pm_variant is not None:
         ctx.set_tuning(ctx.TUNE_PM_VARIANT, args.pm_variant)
+    if args.cg_precond is not None:
+        ctx.set_tuning(ctx.TUNE_CG_PRECOND, args.cg_precond)
     ctx.set_seed(7)
     img, mask, p = workload()
     if args.case == "process":
@@ -485,6 +508,11 @@ def main():
                     help="9x9 PatchMatch window reads: 0 target in shared memory + plain source loads, "
                          "1 source windows staged by tensor copies, 2 target in registers "
                          "(default: the library's)")
+    ap.add_argument("--no-variants", action="store_true",
+                    help="skip the extra measurement with the Jacobi-preconditioned CG")
+    ap.add_argument("--cg-precond", type=int, default=None, choices=[0, 1],
+                    help="NL-Poisson CG: 0 plain (the reference's), 1 Jacobi-preconditioned "
+                         "(default: the library's, 0)")
     ap.add_argument("--batch-count", type=int, default=16,
                     help="images in the batched-vs-plain comparison (0 skips it)")
     ap.add_argument("--batch-max-side", type=int, default=512)

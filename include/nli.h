@@ -403,11 +403,20 @@ int nli_ctx_set_batch_width(nli_ctx *ctx, int width);
  *                                  staged in shared memory by tensor copies;
  *                                  2 target window in registers.  The fields
  *                                  are identical for all three.
+ *   NLI_TUNE_CG_PRECOND            NL-Poisson / NL-depth conjugate gradient:
+ *                                  0 (default) plain CG as the reference
+ *                                  (patch_non_local_poisson.cpp:387-477);
+ *                                  1 Jacobi-preconditioned.  Both stop at
+ *                                  |r|^2 < cg_tol |r0|^2 on the true
+ *                                  residual; 1 needs fewer iterations and
+ *                                  its solution differs within that
+ *                                  tolerance.
  * nli_ctx_get_tuning reads them back. */
 #define NLI_TUNE_CG_CLUSTER_CAP 0
 #define NLI_TUNE_CG_UNKNOWNS_PER_CTA 1
 #define NLI_TUNE_BATCH_WIDTH 2
 #define NLI_TUNE_PM_VARIANT 3
+#define NLI_TUNE_CG_PRECOND 4
 int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value);
 int nli_ctx_get_tuning(nli_ctx *ctx, int knob, int *value);
 /* The seed image `index` of a batch runs with. */

@@ -73,6 +73,12 @@ void fill_dist_args(DistArgs &a, const nli_distance_params &p, int C)
 	std::memcpy(a.weights, w.data(), sizeof(float) * w.size());
 }
 
+void clear_timeout(nli_ctx *ctx)
+{
+	// after a synchronize: no kernel of the context is running
+	NLI_CUDA(cudaMemset(&ctx->status->timeout, 0, sizeof(int)));
+}
+
 }  // namespace nli
 
 using namespace nli;
@@ -581,6 +587,10 @@ int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value)
 		if (value < 0 || value > 2) return NLI_E_INVALID;
 		ctx->tune_pm_variant = value;
 		return NLI_OK;
+	case NLI_TUNE_CG_PRECOND:
+		if (value != 0 && value != 1) return NLI_E_INVALID;
+		ctx->tune_cg_precond = value;
+		return NLI_OK;
 	}
 	return NLI_E_INVALID;
 }
@@ -593,6 +603,7 @@ int nli_ctx_get_tuning(nli_ctx *ctx, int knob, int *value)
 	case NLI_TUNE_CG_UNKNOWNS_PER_CTA: *value = ctx->tune_cg_unknowns_per_cta; return NLI_OK;
 	case NLI_TUNE_BATCH_WIDTH: *value = ctx->batch_width; return NLI_OK;
 	case NLI_TUNE_PM_VARIANT: *value = ctx->tune_pm_variant; return NLI_OK;
+	case NLI_TUNE_CG_PRECOND: *value = ctx->tune_cg_precond; return NLI_OK;
 	}
 	return NLI_E_INVALID;
 }

@@ -121,6 +121,7 @@ struct nli_ctx {
 	int tune_cg_cluster_cap = 16;        // CTAs per CG cluster at most
 	int tune_cg_unknowns_per_cta = 1024; // at least this many unknowns per CG CTA
 	int tune_pm_variant = 0;             // 9x9 PatchMatch window reads (PmVariant)
+	int tune_cg_precond = 0;             // NL-Poisson CG: 0 plain (the reference's), 1 Jacobi
 	int max_smem_optin = 0;              // dynamic shared memory per block at most
 	std::vector<nli_ctx *> workers;
 	std::vector<cudaEvent_t> event_pool;
@@ -200,6 +201,9 @@ struct DistArgs {
 // ---------------------------------------------------------- host helpers
 std::vector<float> gaussian_weights_host(unsigned sx, unsigned sy, float sigma_x, float sigma_y);
 void fill_dist_args(DistArgs &a, const nli_distance_params &p, int C);
+// Resets the device timeout word once a timeout has been read and reported
+// (the stream has been synchronised), so the context stays usable.
+void clear_timeout(nli_ctx *ctx);
 
 // ------------------------------------------------------------- launchers
 // gradient.cu

@@ -987,8 +987,10 @@ void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patch
 			NLI_CUDA(cudaMemcpyAsync(hc + 2, partials + eg, sizeof(double), cudaMemcpyDeviceToHost, s));
 			NLI_CUDA(cudaMemcpyAsync(hc + 3, &ctx->status->timeout, sizeof(int), cudaMemcpyDeviceToHost, s));
 			NLI_CUDA(cudaStreamSynchronize(s));
-			NLI_REQUIRE(*reinterpret_cast<const int *>(hc + 3) == 0, NLI_E_TIMEOUT,
-			            "PatchMatch window copies timed out");
+			if (*reinterpret_cast<const int *>(hc + 3) != 0) {
+				clear_timeout(ctx);
+				NLI_REQUIRE(false, NLI_E_TIMEOUT, "PatchMatch window copies timed out");
+			}
 			ctx->candidates += (int64_t)hc[0];
 			ctx->candidates_partial += (int64_t)hc[1];
 			*energy = *reinterpret_cast<double *>(hc + 2);

@@ -452,21 +452,30 @@ __device__ __forceinline__ float apply_A(const Unknown &n, float lam, const floa
 
 constexpr int kCgBlock = 512;
 
-// Deterministic grid reduction: every block sums the per-block partials in
-// the same order, so all blocks see identical totals.
-__device__ __forceinline__ void reduce_partials(const double *__restrict__ part, int nblocks, int C, double *out,
+// Deterministic grid reduction of the first nv of 8 values per block:
+// every block sums the per-block partials in the same order, so all blocks
+// see identical totals.
+__device__ __forceinline__ void reduce_partials(const double *__restrict__ part, int nblocks, int nv, double *out,
                                                 double *smem)
 {
 	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-	if (wid < C) {
+	if (wid < nv) {
 		double v = 0.0;
-		for (int b = lane; b < nblocks; b += 32) v += __ldcg(part + (size_t)b * 4 + wid);
+		for (int b = lane; b < nblocks; b += 32) v += __ldcg(part + (size_t)b * 8 + wid);
 		v = warp_sum(v);
 		if (lane == 0) smem[wid] = v;
 	}
 	__syncthreads();
-	for (int c = 0; c < C; c++) out[c] = smem[c];
+	for (int c = 0; c < nv; c++) out[c] = smem[c];
 	__syncthreads();
+}
+
+// Jacobi preconditioner of a row of the grid kernel's system (see
+// jacobi_inv of the cluster kernel).
+__device__ __forceinline__ float jacobi_inv_grid(const Unknown &n, float lam)
+{
+	const float dg = lam * n.S + (1.0f - lam) * (n.s_up + n.s_left + n.s_down + n.s_right);
+	return (dg > 0.f) ? 1.0f / dg : 1.0f;
 }
 
 // Conjugate gradient of conjugte_gradient (:387-477) for all channels at
@@ -476,60 +485,74 @@ __device__ __forceinline__ void reduce_partials(const double *__restrict__ part,
 // Vectors are float, inner products double.  The grid is co-resident
 // (cooperative launch) and phases are separated by the bounded barrier.
 // Ends by writing u = orig + x into the image and the partial sums of
-// (u_old - u_new)^2.
+// (u_old - u_new)^2.  PRE: Jacobi-preconditioned as the cluster kernel
+// (z = M r kept in `z`, d = z + beta d, alpha = <r, z> / <z, q>), same
+// stopping test.
+template <bool PRE>
 __global__ void __launch_bounds__(kCgBlock) k_poisson_cg(PoissonArgs a, const Unknown *__restrict__ unk,
                                                          const float *__restrict__ b, float *__restrict__ x,
                                                          float *__restrict__ r, float *__restrict__ d,
-                                                         float *__restrict__ q, double *__restrict__ part,
-                                                         DevStatus *st, int *__restrict__ iters_out,
+                                                         float *__restrict__ q, float *__restrict__ z,
+                                                         double *__restrict__ part, DevStatus *st,
+                                                         int *__restrict__ iters_out,
                                                          const int32_t *__restrict__ hole,
                                                          const float *orig, float *img,
                                                          double *__restrict__ diff_part)
 {
-	__shared__ double red[kCgBlock / 32][4];
-	__shared__ double tot[4];
+	__shared__ double red[kCgBlock / 32][8];
+	__shared__ double tot[8];
 	const int nh = a.nh, C = a.C;
+	const int NV = PRE ? 2 * C : C;  // sums of the residual phase: |r|^2 (and <r, z>)
 	const unsigned nb = gridDim.x;
 	const int stride = gridDim.x * blockDim.x;
-	double *partA = part;                 // [nb][4]
-	double *partB = part + (size_t)nb * 4;  // [nb][4]
+	double *partA = part;                   // [nb][8]
+	double *partB = part + (size_t)nb * 8;  // [nb][8]
+	if (!PRE) z = r;
 
-	auto block_partial = [&](double *v, double *dst) {
-		// v[4] per thread -> dst[blockIdx.x][c]
+	auto block_partial = [&](double *v, double *dst, int nv) {
+		// v[nv] per thread -> dst[blockIdx.x][c]
 		const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-		for (int c = 0; c < C; c++) {
+		for (int c = 0; c < nv; c++) {
 			double s = warp_sum(v[c]);
 			if (lane == 0) red[wid][c] = s;
 		}
 		__syncthreads();
-		if (threadIdx.x < C) {
+		if (threadIdx.x < nv) {
 			double s = 0.0;
 			for (int w = 0; w < kCgBlock / 32; w++) s += red[w][threadIdx.x];
-			__stcg(dst + (size_t)blockIdx.x * 4 + threadIdx.x, s);
+			__stcg(dst + (size_t)blockIdx.x * 8 + threadIdx.x, s);
 		}
 		__syncthreads();
 	};
 
-	// r = b - A x0 ; d = r ; |r0|^2
-	double acc[4] = {0, 0, 0, 0};
+	// r = b - A x0 ; z = M r ; d = z ; |r0|^2 (and <r0, z0>)
+	double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nh; k += stride) {
 		const Unknown n = unk[k];
 		for (int c = 0; c < C; c++) {
 			const float *xc = x + (size_t)c * nh;
 			const float rv = b[(size_t)c * nh + k] - apply_A(n, a.lambda[c], xc, __ldcg(xc + k));
 			__stcg(r + (size_t)c * nh + k, rv);
-			__stcg(d + (size_t)c * nh + k, rv);
 			acc[c] += (double)rv * rv;
+			float zv = rv;
+			if (PRE) {
+				zv = jacobi_inv_grid(n, a.lambda[c]) * rv;
+				__stcg(z + (size_t)c * nh + k, zv);
+				acc[C + c] += (double)rv * zv;
+			}
+			__stcg(d + (size_t)c * nh + k, zv);
 		}
 	}
-	block_partial(acc, partB);
+	block_partial(acc, partB, NV);
 	if (!grid_barrier(st, nb)) return;
-	double nr0[4], nr[4];
-	reduce_partials(partB, nb, C, nr0, &tot[0]);
+	double nr0[4], nr[4], rho[4], t8[8];
+	reduce_partials(partB, nb, NV, t8, &tot[0]);
 	bool active[4];
 	int it[4];
 	for (int c = 0; c < 4; c++) {
-		nr[c] = (c < C) ? nr0[c] : 0.0;
+		nr0[c] = (c < C) ? t8[c] : 0.0;
+		nr[c] = nr0[c];
+		rho[c] = (c < C) ? (PRE ? t8[C + c] : t8[c]) : 0.0;
 		active[c] = (c < C) && (nr0[c] > 0);
 		it[c] = 0;
 	}
@@ -537,8 +560,8 @@ __global__ void __launch_bounds__(kCgBlock) k_poisson_cg(PoissonArgs a, const Un
 		bool any = false;
 		for (int c = 0; c < C; c++) any |= active[c];
 		if (!any) break;
-		// q = A d ; <r, q>
-		for (int c = 0; c < 4; c++) acc[c] = 0.0;
+		// q = A d ; <z, q>
+		for (int c = 0; c < 8; c++) acc[c] = 0.0;
 		for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nh; k += stride) {
 			const Unknown n = unk[k];
 			for (int c = 0; c < C; c++) {
@@ -546,18 +569,20 @@ __global__ void __launch_bounds__(kCgBlock) k_poisson_cg(PoissonArgs a, const Un
 				const float *dc = d + (size_t)c * nh;
 				const float qv = apply_A(n, a.lambda[c], dc, __ldcg(dc + k));
 				__stcg(q + (size_t)c * nh + k, qv);
-				acc[c] += (double)__ldcg(r + (size_t)c * nh + k) * qv;
+				acc[c] += (double)__ldcg(z + (size_t)c * nh + k) * qv;
 			}
 		}
-		block_partial(acc, partA);
+		block_partial(acc, partA, C);
 		if (!grid_barrier(st, nb)) return;
-		double rq[4];
+		double rq[8];
 		reduce_partials(partA, nb, C, rq, &tot[0]);
 		float alpha[4];
-		for (int c = 0; c < C; c++) alpha[c] = active[c] ? (float)(nr[c] / rq[c]) : 0.f;
-		// x += alpha d ; r -= alpha q ; |r|^2
-		for (int c = 0; c < 4; c++) acc[c] = 0.0;
+		for (int c = 0; c < C; c++) alpha[c] = active[c] ? (float)(rho[c] / rq[c]) : 0.f;
+		// x += alpha d ; r -= alpha q ; z = M r ; |r|^2 (and <r, z>)
+		for (int c = 0; c < 8; c++) acc[c] = 0.0;
 		for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nh; k += stride) {
+			Unknown n;
+			if (PRE) n = unk[k];
 			for (int c = 0; c < C; c++) {
 				if (!active[c]) continue;
 				const size_t o = (size_t)c * nh + k;
@@ -566,23 +591,32 @@ __global__ void __launch_bounds__(kCgBlock) k_poisson_cg(PoissonArgs a, const Un
 				const float rv = __ldcg(r + o) - alpha[c] * __ldcg(q + o);
 				__stcg(r + o, rv);
 				acc[c] += (double)rv * rv;
+				if (PRE) {
+					const float zv = jacobi_inv_grid(n, a.lambda[c]) * rv;
+					__stcg(z + o, zv);
+					acc[C + c] += (double)rv * zv;
+				}
 			}
 		}
-		block_partial(acc, partB);
+		block_partial(acc, partB, NV);
 		if (!grid_barrier(st, nb)) return;
-		double nrn[4];
-		reduce_partials(partB, nb, C, nrn, &tot[0]);
+		double nrn[8];
+		reduce_partials(partB, nb, NV, nrn, &tot[0]);
 		float beta[4];
 		for (int c = 0; c < C; c++) {
-			beta[c] = active[c] ? (float)(nrn[c] / nr[c]) : 0.f;
-			if (active[c]) nr[c] = nrn[c];
+			const double rhon = PRE ? nrn[C + c] : nrn[c];
+			beta[c] = active[c] ? (float)(rhon / rho[c]) : 0.f;
+			if (active[c]) {
+				nr[c] = nrn[c];
+				rho[c] = rhon;
+			}
 		}
-		// d = r + beta d
+		// d = z + beta d
 		for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nh; k += stride) {
 			for (int c = 0; c < C; c++) {
 				if (!active[c]) continue;
 				const size_t o = (size_t)c * nh + k;
-				__stcg(d + o, __ldcg(r + o) + beta[c] * __ldcg(d + o));
+				__stcg(d + o, __ldcg(z + o) + beta[c] * __ldcg(d + o));
 			}
 		}
 		for (int c = 0; c < C; c++) {
@@ -667,22 +701,39 @@ __global__ void k_poisson_compact(const Unknown *__restrict__ unk, int nh, int c
 	out[k] = c;
 }
 
-template <int C>
+// 1 / the diagonal of an unknown's row, lam S + (1 - lam) (sum of its four
+// link coefficients) (1 where that is not positive): the Jacobi
+// preconditioner of the PRE kernels.
+__device__ __forceinline__ float jacobi_inv(const UnkC &n, float lam)
+{
+	const float sum = n.s_up + n.s_left + ((n.links & 1) ? n.S : 0.f) + ((n.links & 2) ? n.S : 0.f);
+	const float dg = lam * n.S + (1.0f - lam) * sum;
+	return (dg > 0.f) ? 1.0f / dg : 1.0f;
+}
+
+// PRE: Jacobi-preconditioned CG (NLI_TUNE_CG_PRECOND): z = M r with M the
+// inverse diagonal, d = z + beta d_old, alpha = <r, z> / <z, A d>, beta =
+// <r', z'> / <r, z>.  The stopping test stays |r|^2 < tol |r0|^2 on the
+// true residual, so the solve ends at the same residual as the plain CG,
+// in fewer iterations.  Without PRE, z is r itself and the iteration is the
+// reference's.
+template <int C, bool PRE>
 __global__ void __launch_bounds__(kClusterBlock, 1)
     k_poisson_cg_cluster(PoissonArgs a, int chunk, const UnkC *__restrict__ unk_g, const float *__restrict__ b,
                          const float *__restrict__ x0, int *__restrict__ iters_out, const int32_t *__restrict__ hole,
                          const float *orig, float *img, double *__restrict__ diff_part)
 {
+	constexpr int NV = PRE ? 2 * C : C;  // sums of the residual phase: |r|^2 (and <r, z>)
 	const int Ctot = a.C;
 	namespace cgs = cooperative_groups;
 	cgs::cluster_group cluster = cgs::this_cluster();
 	extern __shared__ float smem[];
-	__shared__ double red[kClusterBlock / 32][4];
-	__shared__ double partA[4], partB[4], tot[4];
+	__shared__ double red[kClusterBlock / 32][8];
+	__shared__ double partA[8], partB[8], tot[8];
 	__shared__ float s_coef[4];
 	__shared__ int s_active[4];
-	__shared__ double s_nr[4];
-	__shared__ float *base[3][kClusterMax];  // r, dA, dB of every CTA
+	__shared__ double s_nr[4], s_rho[4];
+	__shared__ float *base[3][kClusterMax];  // z (r without PRE), dA, dB of every CTA
 	const int rank = (int)cluster.block_rank(), ncta = (int)cluster.num_blocks();
 	const int group = (int)blockIdx.x / ncta, cb = group * C;  // this cluster's first channel
 	b += (size_t)cb * a.nh;
@@ -692,52 +743,56 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 	const size_t vlen = (size_t)C * chunk;
 	float *s_r = smem, *s_dA = smem + vlen, *s_dB = smem + 2 * vlen, *s_x = smem + 3 * vlen;
-	UnkC *s_unk = reinterpret_cast<UnkC *>(smem + kClusterVectors * vlen);
+	float *s_z = PRE ? smem + 4 * vlen : s_r;
+	UnkC *s_unk = reinterpret_cast<UnkC *>(smem + (kClusterVectors + (PRE ? 1 : 0)) * vlen);
 	if (threadIdx.x < ncta) {
-		base[0][threadIdx.x] = cluster.map_shared_rank(s_r, (int)threadIdx.x);
+		base[0][threadIdx.x] = cluster.map_shared_rank(s_z, (int)threadIdx.x);
 		base[1][threadIdx.x] = cluster.map_shared_rank(s_dA, (int)threadIdx.x);
 		base[2][threadIdx.x] = cluster.map_shared_rank(s_dB, (int)threadIdx.x);
 	}
 	for (int l = threadIdx.x; l < own; l += blockDim.x) s_unk[l] = unk_g[lo + l];
 	__syncthreads();
 
-	// block partial sums per channel into dst (written by warp 0; read by
-	// the other CTAs after the next cluster barrier)
-	auto block_reduce = [&](const float *v, double *dst) {
+	// block partial sums of the first nv values into dst (written by warp 0;
+	// read by the other CTAs after the next cluster barrier)
+	auto block_reduce = [&](const float *v, double *dst, int nv) {
 #pragma unroll
-		for (int c = 0; c < C; c++) {
+		for (int c = 0; c < NV; c++) {
+			if (c >= nv) break;
 			const float s = warp_sum(v[c]);
 			if (lane == 0) red[wid][c] = (double)s;
 		}
 		__syncthreads();
 		if (wid == 0) {
 #pragma unroll
-			for (int c = 0; c < C; c++) {
+			for (int c = 0; c < NV; c++) {
+				if (c >= nv) break;
 				const double s = warp_sum((lane < kClusterBlock / 32) ? red[lane][c] : 0.0);
 				if (lane == 0) dst[c] = s;
 			}
 		}
 	};
-	// cluster totals of the block partials src, in rank order, left in every
-	// lane of warp 0 (call from warp 0 only, after a cluster barrier)
-	auto warp0_totals = [&](const double *src, double *out) {
+	// cluster totals of the first nv block partials src, in rank order, left
+	// in every lane of warp 0 (call from warp 0 only, after a cluster barrier)
+	auto warp0_totals = [&](const double *src, double *out, int nv) {
 #pragma unroll
-		for (int c = 0; c < C; c++) {
+		for (int c = 0; c < NV; c++) {
+			if (c >= nv) break;
 			const double v = warp_sum((lane < ncta) ? cluster.map_shared_rank(const_cast<double *>(src), lane)[c] : 0.0);
 			out[c] = __shfl_sync(0xffffffffu, v, 0);
 		}
 	};
-	// channel values of vector `v` (0: r, 1: dA, 2: dB) at a 16-bit code
+	// channel values of vector `v` (0: z, 1: dA, 2: dB) at a 16-bit code
 	auto nb = [&](int v, uint32_t code) -> const float * {
 		const int o = (int)(code >> 12), l = (int)(code & 0xFFF);
-		const float *bp = (o == rank) ? (v == 0 ? s_r : v == 1 ? s_dA : s_dB) : base[v][o];
+		const float *bp = (o == rank) ? (v == 0 ? s_z : v == 1 ? s_dA : s_dB) : base[v][o];
 		return bp + (size_t)l * C;
 	};
 
 	// r0 = b - A x0 (x0 from global: neighbours may belong to other CTAs)
-	float facc[4];
+	float facc[8];
 #pragma unroll
-	for (int c = 0; c < 4; c++) facc[c] = 0.f;
+	for (int c = 0; c < 8; c++) facc[c] = 0.f;
 	for (int l = threadIdx.x; l < own; l += blockDim.x) {
 		const int k = lo + l;
 		const UnkC n = s_unk[l];
@@ -761,26 +816,35 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 			s_dA[(size_t)l * C + c] = 0.f;
 			s_x[(size_t)l * C + c] = xk;
 			facc[c] = fmaf(rv, rv, facc[c]);
+			if (PRE) {
+				const float zv = jacobi_inv(n, a.lambda[cb + c]) * rv;
+				s_z[(size_t)l * C + c] = zv;
+				facc[C + c] = fmaf(rv, zv, facc[C + c]);
+			}
 		}
 	}
-	block_reduce(facc, partB);
+	block_reduce(facc, partB, NV);
 	cluster.sync();
-	double nr0[4], nr[4];
+	double nr0[4], nr[4], rho[4];
 	if (wid == 0) {
-		double t[4];
-		warp0_totals(partB, t);
+		double t[8];
+		warp0_totals(partB, t, NV);
 		if (lane == 0)
-			for (int c = 0; c < C; c++) tot[c] = t[c];
+			for (int c = 0; c < NV; c++) tot[c] = t[c];
 	}
 	__syncthreads();
 #pragma unroll
-	for (int c = 0; c < C; c++) nr0[c] = tot[c];
+	for (int c = 0; c < C; c++) {
+		nr0[c] = tot[c];
+		rho[c] = PRE ? tot[C + c] : tot[c];
+	}
 	bool active[4];
 	int it[4];
 	float beta[4];
 #pragma unroll
 	for (int c = 0; c < 4; c++) {
 		nr[c] = (c < C) ? nr0[c] : 0.0;
+		if (c >= C) rho[c] = 0.0;
 		active[c] = (c < C) && (nr0[c] > 0);
 		it[c] = 0;
 		beta[c] = 0.f;
@@ -793,9 +857,9 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 		for (int c = 0; c < C; c++) any |= active[c];
 		if (!any) break;
 		float *dold = h ? s_dB : s_dA, *dnew = h ? s_dA : s_dB;
-		// d = r + beta d_old (own and neighbours) ; q = A d ; <r, q>
+		// d = z + beta d_old (own and neighbours) ; q = A d ; <z, q>
 #pragma unroll
-		for (int c = 0; c < 4; c++) facc[c] = 0.f;
+		for (int c = 0; c < 8; c++) facc[c] = 0.f;
 #pragma unroll
 		for (int u = 0; u < kClusterPerThread; u++) {
 			const int l = threadIdx.x + u * kClusterBlock;
@@ -814,7 +878,7 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 			for (int c = 0; c < C; c++) {
 				if (!active[c]) continue;
 				const size_t o = (size_t)l * C + c;
-				const float rk = s_r[o];
+				const float rk = s_z[o];
 				const float dk = rk + beta[c] * dold[o];
 				float lap = -dk * sum;
 #pragma unroll
@@ -826,26 +890,32 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 				facc[c] = fmaf(rk, qv, facc[c]);
 			}
 		}
-		block_reduce(facc, partA);
+		block_reduce(facc, partA, C);
 		cluster.sync();
 		if (wid == 0) {
 			double rq[4];
-			warp0_totals(partA, rq);
+			warp0_totals(partA, rq, C);
 #pragma unroll
 			for (int c = 0; c < C; c++)
-				if (lane == c) s_coef[c] = active[c] ? (float)(nr[c] / rq[c]) : 0.f;
+				if (lane == c) s_coef[c] = active[c] ? (float)(rho[c] / rq[c]) : 0.f;
 		}
 		__syncthreads();
 		float alpha[4];
 #pragma unroll
 		for (int c = 0; c < C; c++) alpha[c] = s_coef[c];
-		// x += alpha d ; r -= alpha q ; |r|^2   (own unknowns only)
+		// x += alpha d ; r -= alpha q ; z = M r ; |r|^2 (and <r, z>)   (own unknowns only)
 #pragma unroll
-		for (int c = 0; c < 4; c++) facc[c] = 0.f;
+		for (int c = 0; c < 8; c++) facc[c] = 0.f;
 #pragma unroll
 		for (int u = 0; u < kClusterPerThread; u++) {
 			const int l = threadIdx.x + u * kClusterBlock;
 			if (l >= own) break;
+			float minv[C];
+			if (PRE) {
+				const UnkC n = s_unk[l];
+#pragma unroll
+				for (int c = 0; c < C; c++) minv[c] = jacobi_inv(n, a.lambda[cb + c]);
+			}
 #pragma unroll
 			for (int c = 0; c < C; c++) {
 				if (!active[c]) continue;
@@ -854,19 +924,26 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 				const float rv = s_r[o] - alpha[c] * q[u][c];
 				s_r[o] = rv;
 				facc[c] = fmaf(rv, rv, facc[c]);
+				if (PRE) {
+					const float zv = minv[c] * rv;
+					s_z[o] = zv;
+					facc[C + c] = fmaf(rv, zv, facc[C + c]);
+				}
 			}
 		}
 		// partA / partB are rewritten only after the next cluster barrier,
 		// by which time every CTA has read them
-		block_reduce(facc, partB);
+		block_reduce(facc, partB, NV);
 		cluster.sync();
 		if (wid == 0) {
-			double nrn[4];
-			warp0_totals(partB, nrn);
+			double nrn[8];
+			warp0_totals(partB, nrn, NV);
 #pragma unroll
 			for (int c = 0; c < C; c++)
 				if (lane == c && active[c]) {
-					s_coef[c] = (float)(nrn[c] / nr[c]);
+					const double rhon = PRE ? nrn[C + c] : nrn[c];
+					s_coef[c] = (float)(rhon / rho[c]);
+					s_rho[c] = rhon;
 					s_nr[c] = nrn[c];
 					s_active[c] = ((nrn[c] < (double)a.tol * nr0[c]) || (it[c] >= a.limit)) ? 0 : 1;
 				}
@@ -879,6 +956,7 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 			if (!active[c]) continue;
 			beta[c] = s_coef[c];
 			nr[c] = s_nr[c];
+			rho[c] = s_rho[c];
 			it[c]++;
 			active[c] = s_active[c] != 0;
 		}
@@ -926,7 +1004,10 @@ static double read_total(nli_ctx *ctx, double *partials, int n, int *cg_iters_de
 	// copies, CG grid barriers)
 	NLI_CUDA(cudaMemcpyAsync(h + 128, &ctx->status->timeout, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
 	NLI_CUDA(cudaStreamSynchronize(ctx->stream));
-	NLI_REQUIRE(*reinterpret_cast<const int *>(h + 128) == 0, NLI_E_TIMEOUT, "a device-side wait timed out");
+	if (*reinterpret_cast<const int *>(h + 128) != 0) {
+		clear_timeout(ctx);
+		NLI_REQUIRE(false, NLI_E_TIMEOUT, "a device-side wait timed out");
+	}
 	if (cg_iters_dev) {
 		const int *it = reinterpret_cast<const int *>(h + 64);
 		for (int c = 0; c < C; c++) {
@@ -937,12 +1018,23 @@ static double read_total(nli_ctx *ctx, double *partials, int n, int *cg_iters_de
 	return *reinterpret_cast<double *>(h);
 }
 
-static void (*cluster_kernel(int CC))(PoissonArgs, int, const UnkC *, const float *, const float *, int *,
-                                      const int32_t *, const float *, float *, double *)
+static void (*cluster_kernel(int CC, bool pre))(PoissonArgs, int, const UnkC *, const float *, const float *, int *,
+                                                const int32_t *, const float *, float *, double *)
 {
-	return (CC == 1) ? k_poisson_cg_cluster<1>
-	       : (CC == 2) ? k_poisson_cg_cluster<2> : (CC == 3) ? k_poisson_cg_cluster<3> : k_poisson_cg_cluster<4>;
+	if (pre)
+		return (CC == 1)   ? k_poisson_cg_cluster<1, true>
+		       : (CC == 2) ? k_poisson_cg_cluster<2, true>
+		       : (CC == 3) ? k_poisson_cg_cluster<3, true>
+		                   : k_poisson_cg_cluster<4, true>;
+	return (CC == 1)   ? k_poisson_cg_cluster<1, false>
+	       : (CC == 2) ? k_poisson_cg_cluster<2, false>
+	       : (CC == 3) ? k_poisson_cg_cluster<3, false>
+	                   : k_poisson_cg_cluster<4, false>;
 }
+
+// Vectors of `chunk` floats per channel a cluster CTA keeps in shared
+// memory: r, two direction buffers, x (and z when preconditioned).
+static int cluster_vectors(bool pre) { return kClusterVectors + (pre ? 1 : 0); }
 
 // Coefficients (gather), the compact system and its right-hand side b and
 // start x0 = image - orig (patch_non_local_poisson.cpp:36-82).  Chooses the
@@ -1000,17 +1092,19 @@ static PoissonSystem poisson_system(nli_ctx *ctx, const UpdArgs &u, const nli_up
 		// largest cluster the device runs with the biggest shared-memory footprint
 		int maxc = 0;
 		bool ok = true;
-		for (int CC = 1; CC <= 4; CC++) {
-			ok &= cudaFuncSetAttribute(cluster_kernel(CC), cudaFuncAttributeNonPortableClusterSizeAllowed, 1) == 0;
-			ok &= cudaFuncSetAttribute(cluster_kernel(CC), cudaFuncAttributeMaxDynamicSharedMemorySize,
-			                           (int)kSmemBudget) == 0;
-		}
+		for (int CC = 1; CC <= 4; CC++)
+			for (int pre = 0; pre < 2; pre++) {
+				ok &= cudaFuncSetAttribute(cluster_kernel(CC, pre), cudaFuncAttributeNonPortableClusterSizeAllowed,
+				                           1) == 0;
+				ok &= cudaFuncSetAttribute(cluster_kernel(CC, pre), cudaFuncAttributeMaxDynamicSharedMemorySize,
+				                           (int)kSmemBudget) == 0;
+			}
 		if (ok) {
 			cudaLaunchConfig_t qc = {};
 			qc.gridDim = dim3(kClusterMax);
 			qc.blockDim = dim3(kClusterBlock);
 			qc.dynamicSmemBytes = kSmemBudget;
-			if (cudaOccupancyMaxPotentialClusterSize(&maxc, cluster_kernel(4), &qc) != cudaSuccess) maxc = 0;
+			if (cudaOccupancyMaxPotentialClusterSize(&maxc, cluster_kernel(4, true), &qc) != cudaSuccess) maxc = 0;
 		}
 		cudaGetLastError();
 		ctx->cg_cluster_max = std::min(maxc, kClusterMax);
@@ -1019,7 +1113,8 @@ static PoissonSystem poisson_system(nli_ctx *ctx, const UpdArgs &u, const nli_up
 		const int per = std::max(1, ctx->tune_cg_unknowns_per_cta);
 		P.ncta = std::max(1, std::min(std::min(ctx->cg_cluster_max, ctx->tune_cg_cluster_cap), (nh + per - 1) / per));
 		P.chunk = (nh + P.ncta - 1) / P.ncta;
-		if ((size_t)kClusterVectors * P.chunk * sizeof(float) + P.chunk * sizeof(UnkC) > kSmemBudget ||
+		if ((size_t)cluster_vectors(ctx->tune_cg_precond) * P.chunk * sizeof(float) + P.chunk * sizeof(UnkC) >
+		        kSmemBudget ||
 		    P.chunk > kClusterMaxChunk)
 			P.ncta = P.chunk = 0;
 	}
@@ -1041,7 +1136,8 @@ static int poisson_solve(nli_ctx *ctx, PoissonSystem &P, const int32_t *hole, co
 	const int nh = P.pa.nh, C = P.pa.C;
 	int *iters = ctx->buf<int>("poi.iters", 4);
 	if (P.ncta > 0) {
-		const size_t smem = (size_t)kClusterVectors * P.chunk * sizeof(float) + P.chunk * sizeof(UnkC);
+		const bool pre = ctx->tune_cg_precond != 0;
+		const size_t smem = (size_t)cluster_vectors(pre) * P.chunk * sizeof(float) + P.chunk * sizeof(UnkC);
 		UnkC *unkc = ctx->buf<UnkC>("poi.unkc", nh);
 		k_poisson_compact<<<(nh + 255) / 256, 256, 0, s>>>(P.unk, nh, P.chunk, unkc);
 		NLI_CHECK_LAUNCH();
@@ -1059,31 +1155,37 @@ static int poisson_solve(nli_ctx *ctx, PoissonSystem &P, const int32_t *hole, co
 		cfg.attrs = attr;
 		cfg.numAttrs = 1;
 		ProfScope ps(ctx, "poisson_cg");
-		NLI_CUDA(cudaLaunchKernelEx(&cfg, cluster_kernel(1), P.pa, P.chunk, (const UnkC *)unkc, (const float *)P.b,
+		NLI_CUDA(cudaLaunchKernelEx(&cfg, cluster_kernel(1, pre), P.pa, P.chunk, (const UnkC *)unkc, (const float *)P.b,
 		                            (const float *)P.x, iters, hole, orig, img, diff_part));
 		nli_count_launch_internal();
 		return C * P.ncta;
 	}
 	int dev_blocks_per_sm = 0;
-	NLI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&dev_blocks_per_sm, k_poisson_cg, kCgBlock, 0));
+	const bool pre = ctx->tune_cg_precond != 0;
+	const void *kern = pre ? (const void *)k_poisson_cg<true> : (const void *)k_poisson_cg<false>;
+	NLI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&dev_blocks_per_sm, kern, kCgBlock, 0));
 	const int max_blocks = dev_blocks_per_sm * ctx->num_sms;
 	NLI_REQUIRE(max_blocks > 0, NLI_E_CUDA, "conjugate gradient kernel cannot be made resident");
 	int grid = (nh + kCgBlock - 1) / kCgBlock;
 	grid = std::min(std::max(grid, 1), std::min(max_blocks, ctx->num_sms));
-	double *part = ctx->buf<double>("poi.part", (size_t)grid * 8);
+	double *part = ctx->buf<double>("poi.part", (size_t)grid * 16);
 	double *diff_part = ctx->buf<double>("poi.diff", grid + 1);
 	float *r = ctx->buf<float>("poi.r", (size_t)nh * C);
 	float *d = ctx->buf<float>("poi.d", (size_t)nh * C);
 	float *q = ctx->buf<float>("poi.q", (size_t)nh * C);
-	NLI_CUDA(cudaMemsetAsync(ctx->status, 0, sizeof(DevStatus), s));
+	float *z = pre ? ctx->buf<float>("poi.z", (size_t)nh * C) : nullptr;
+	// the grid barrier's counters (the timeout word is left for the
+	// iteration's readback)
+	NLI_CUDA(cudaMemsetAsync(ctx->status, 0, offsetof(DevStatus, timeout), s));
 	DevStatus *st = ctx->status;
 	const Unknown *unk = P.unk;
 	const float *b = P.b;
 	float *x = P.x;
-	void *args[] = {&P.pa, &unk, &b, &x, &r, &d, &q, &part, &st, &iters, (void *)&hole, &orig, &img, &diff_part};
+	void *args[] = {&P.pa, &unk, &b,   &x,     (void *)&r, &d, &q, &z, &part, &st, &iters, (void *)&hole,
+	                &orig, &img, &diff_part};
 	{
 		ProfScope ps(ctx, "poisson_cg");
-		NLI_CUDA(cudaLaunchCooperativeKernel((const void *)k_poisson_cg, dim3(grid), dim3(kCgBlock), args, 0, s));
+		NLI_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kCgBlock), args, 0, s));
 		nli_count_launch_internal();
 	}
 	return grid;
