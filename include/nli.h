@@ -421,6 +421,13 @@ int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value);
 int nli_ctx_get_tuning(nli_ctx *ctx, int knob, int *value);
 /* The seed image `index` of a batch runs with. */
 uint64_t nli_batch_seed(uint64_t seed, int index);
+/* Host-side fault injection for tests: the `countdown`-th next growth of
+ * the context's device workspace fails with NLI_E_NOMEM ("device
+ * allocation failed (injected)") without calling cudaMalloc; 0 disarms.
+ * The reference has no allocation failure path of its own (its containers
+ * throw std::bad_alloc); this one checks that a failed call leaves the
+ * context usable. */
+int nli_debug_fail_allocation(nli_ctx *ctx, int countdown);
 
 #ifdef __cplusplus
 }

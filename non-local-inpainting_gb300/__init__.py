@@ -104,6 +104,7 @@ def load(path=LIB_PATH):
     proto("nli_process_batch_device", I, [P, I, prp, P, P, P, P, P, P, st, P])
     proto("nli_ctx_set_batch_width", I, [P, I])
     proto("nli_batch_seed", ct.c_uint64, [ct.c_uint64, I])
+    proto("nli_debug_fail_allocation", I, [P, I])
     proto("nli_ctx_set_tuning", I, [P, I, I])
     proto("nli_ctx_get_tuning", I, [P, I, ct.POINTER(I)])
     proto("nli_launch_count", ct.c_int64, [])
@@ -492,6 +493,11 @@ class Context:
 
     def batch_seed(self, seed, index):
         return int(self.lib.nli_batch_seed(seed, index))
+
+    def fail_allocation(self, countdown):
+        """Test hook: the countdown-th next workspace growth fails with
+        NLI_E_NOMEM (nli_debug_fail_allocation); 0 disarms."""
+        self._check(self.lib.nli_debug_fail_allocation(self.h, countdown))
 
     def process_device(self, img, mask, params, out=None):
         """ImageInpainting::process on device tensors; returns (out, stats)."""

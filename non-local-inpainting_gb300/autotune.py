@@ -122,6 +122,51 @@ def tune_batch_width(ctx, items, params, widths=(2, 4, 8, 12, 16)):
     return {"best": choice, "ms": times}
 
 
+def device_key(device=0):
+    """The cache key of a device: its name, SM count and compute capability."""
+    import torch
+    pr = torch.cuda.get_device_properties(device)
+    return "%s|%d SMs|sm_%d%d" % (pr.name, pr.multi_processor_count, pr.major, pr.minor)
+
+
+def save(path, key, cg=None, batch_width=None, pm_variant=None):
+    """Stores the choices for one device key in a JSON cache file (other
+    devices' entries are kept)."""
+    import json
+    import os
+    table = {}
+    if os.path.exists(path):
+        with open(path) as f:
+            table = json.load(f)
+    entry = {}
+    if cg is not None:
+        entry["cg"] = [int(cg[0]), int(cg[1])]
+    if batch_width is not None:
+        entry["batch_width"] = int(batch_width)
+    if pm_variant is not None:
+        entry["pm_variant"] = int(pm_variant)
+    table[key] = entry
+    tmp = path + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(table, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+
+
+def load(ctx, path, key):
+    """Applies the cached choices of `key` to ctx; returns them, or None
+    when the file or the key is absent."""
+    import json
+    import os
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        entry = json.load(f).get(key)
+    if entry is None:
+        return None
+    apply(ctx, cg=entry.get("cg"), batch_width=entry.get("batch_width"), pm_variant=entry.get("pm_variant"))
+    return entry
+
+
 def apply(ctx, cg=None, batch_width=None, pm_variant=None):
     """Re-applies stored choices: cg = (cap, unknowns per CTA)."""
     if cg is not None:

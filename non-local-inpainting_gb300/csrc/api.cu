@@ -567,6 +567,13 @@ int nli_ctx_set_batch_width(nli_ctx *ctx, int width)
 
 uint64_t nli_batch_seed(uint64_t seed, int index) { return batch_seed(seed, index); }
 
+int nli_debug_fail_allocation(nli_ctx *ctx, int countdown)
+{
+	if (!ctx || countdown < 0) return NLI_E_INVALID;
+	ctx->fail_alloc_countdown = countdown;
+	return NLI_OK;
+}
+
 int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value)
 {
 	if (!ctx) return NLI_E_INVALID;

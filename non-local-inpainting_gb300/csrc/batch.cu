@@ -95,6 +95,9 @@ void process_batch_run(nli_ctx *ctx, int n, const nli_process_params *params, co
 				NLI_REQUIRE(images[i] && masks[i] && outputs[i], NLI_E_INVALID, "null pointer argument");
 				NLI_REQUIRE(W > 0 && H > 0, NLI_E_INVALID, "image sizes must be positive");
 				NLI_REQUIRE(C >= 1 && C <= 4, NLI_E_UNSUPPORTED, "images must have 1 to 4 channels");
+				char label[48];
+				std::snprintf(label, sizeof(label), "batch image %d", i);
+				NvtxRange image_range(label);
 				w->seed = batch_seed(ctx->seed, i);
 				w->call_counter = 0;
 				nli_process_stats *st = stats ? stats + i : nullptr;

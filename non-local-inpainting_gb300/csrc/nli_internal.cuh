@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>  // header-only NVTX v3: ranges cost nothing without a tool attached
 #include <stdint.h>
 
 #include <algorithm>
@@ -152,14 +153,31 @@ struct nli_ctx {
 		}
 	}
 
+	// Host-side fault injection (nli_debug_fail_allocation): when > 0, the
+	// workspace growth that brings it to 0 fails as an out-of-memory error
+	// without calling cudaMalloc.
+	int fail_alloc_countdown = 0;
+
 	template <class T>
 	T *buf(const std::string &name, size_t count)
 	{
-		return static_cast<T *>(bufs[name].ensure(count * sizeof(T)));
+		nli::DevBuf &b = bufs[name];
+		const size_t n = count * sizeof(T);
+		if (n > b.bytes && fail_alloc_countdown > 0 && --fail_alloc_countdown == 0)
+			throw ::nli::Error{NLI_E_NOMEM, "device allocation failed (injected)"};
+		return static_cast<T *>(b.ensure(n));
 	}
 };
 
 namespace nli {
+
+// NVTX range for profilers (scales, iterations, batch images).
+struct NvtxRange {
+	explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+	~NvtxRange() { nvtxRangePop(); }
+	NvtxRange(const NvtxRange &) = delete;
+	NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 // Times the kernels launched in its lifetime under `name` when the
 // context's profiling is on (events on the context stream).

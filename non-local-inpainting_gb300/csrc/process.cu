@@ -175,7 +175,11 @@ struct Driver {
 		const int32_t *nnf = initial;
 		double total = DBL_MAX;
 		int i;
+		char label[64];
+		std::snprintf(label, sizeof(label), "scale %d (%dx%d)", l, L.W, L.H);
+		NvtxRange scale_range(label);
 		for (i = 0; i < p.iterations && total > p.tolerance; i++) {
+			NvtxRange iteration_range("iteration");
 			int32_t *out = (nnf == bufs[cur]) ? bufs[1 - cur] : bufs[cur];
 			pm(L.img, L.src_eroded, L, nnf, out);
 			nnf = out;

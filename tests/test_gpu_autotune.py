@@ -45,3 +45,21 @@ def test_tuning_knobs_validate(gpu_ctx):
     gpu_ctx.set_tuning(gpu_ctx.TUNE_BATCH_WIDTH, 5)
     assert gpu_ctx.get_tuning(gpu_ctx.TUNE_BATCH_WIDTH) == 5
     gpu_ctx.set_tuning(gpu_ctx.TUNE_BATCH_WIDTH, 8)
+
+
+def test_cache_file_round_trip(gpu_ctx, tmp_path):
+    from nli_gb300 import autotune
+    path = str(tmp_path / "tuning.json")
+    key = autotune.device_key(0)
+    assert autotune.load(gpu_ctx, path, key) is None
+    autotune.save(path, "other device", cg=(8, 512))
+    autotune.save(path, key, cg=(12, 2048), batch_width=6, pm_variant=0)
+    try:
+        got = autotune.load(gpu_ctx, path, key)
+        assert got == {"cg": [12, 2048], "batch_width": 6, "pm_variant": 0}
+        assert gpu_ctx.get_tuning(gpu_ctx.TUNE_CG_CLUSTER_CAP) == 12
+        assert gpu_ctx.get_tuning(gpu_ctx.TUNE_CG_UNKNOWNS_PER_CTA) == 2048
+        assert gpu_ctx.get_tuning(gpu_ctx.TUNE_BATCH_WIDTH) == 6
+        assert autotune.load(gpu_ctx, path, "missing") is None
+    finally:
+        autotune.apply(gpu_ctx, cg=(16, 1024), batch_width=8, pm_variant=0)

@@ -76,3 +76,33 @@ def test_batch_reports_failed_image(gpu_ctx):
 
 def test_empty_batch(gpu_ctx):
     assert gpu_ctx.process_batch([], []) == ([], [])
+
+
+def test_injected_allocation_failure_leaves_context_usable():
+    """Host-side fault injection: a workspace growth fails as out of memory
+    in the middle of process(); the call returns NLI_E_NOMEM with its
+    message, and the same context then runs the image to the same output as
+    a fresh context."""
+    import nli_gb300 as pkg
+    from nli_gb300 import NliError
+    from nli_gb300 import workloads as wl
+    img, mask, _ = wl.config2(seed=6, size=96, scales=3)
+    p = wl.params("nlpoisson", scales=3, coarse=0.5, iters=4, cg_tol=1e-4)
+    ctx = pkg.Context(0)
+    try:
+        ctx.fail_allocation(5)
+        with pytest.raises(NliError) as e:
+            ctx.process(img, mask, p)
+        assert e.value.status == -8 and "injected" in str(e.value)  # NLI_E_NOMEM
+        ctx.fail_allocation(0)
+        ctx.set_seed(3)
+        out, _ = ctx.process(img, mask, p)
+    finally:
+        ctx.close()
+    fresh = pkg.Context(0)
+    try:
+        fresh.set_seed(3)
+        ref, _ = fresh.process(img, mask, p)
+    finally:
+        fresh.close()
+    assert np.array_equal(out, ref)
