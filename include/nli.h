@@ -129,6 +129,8 @@ typedef struct nli_process_stats {
 	int64_t update_calls;
 	int64_t cg_iterations;               /* summed over channels and solves */
 	int64_t candidates;                  /* patch distances evaluated by PatchMatch */
+	int64_t graph_iterations;            /* of the iterations, those run in captured loops
+	                                        (NLI_TUNE_GRAPH_LOOP) */
 } nli_process_stats;
 
 typedef struct nli_ctx nli_ctx;
@@ -411,12 +413,24 @@ int nli_ctx_set_batch_width(nli_ctx *ctx, int width);
  *                                  residual; 1 needs fewer iterations and
  *                                  its solution differs within that
  *                                  tolerance.
+ *   NLI_TUNE_GRAPH_LOOP            1 (default): after the first iteration of
+ *                                  a scale, nli_process(_device) runs the
+ *                                  remaining PatchMatch / update iterations
+ *                                  as one CUDA graph whose while node tests
+ *                                  the stopping rule on the device (no host
+ *                                  round trip per iteration); batches keep
+ *                                  the host loop, where other images' work
+ *                                  hides the round trips.  2: the graph in
+ *                                  batches too.  0: the host loop everywhere.
+ *                                  Identical results; the graph is not used
+ *                                  while profiling is on.
  * nli_ctx_get_tuning reads them back. */
 #define NLI_TUNE_CG_CLUSTER_CAP 0
 #define NLI_TUNE_CG_UNKNOWNS_PER_CTA 1
 #define NLI_TUNE_BATCH_WIDTH 2
 #define NLI_TUNE_PM_VARIANT 3
 #define NLI_TUNE_CG_PRECOND 4
+#define NLI_TUNE_GRAPH_LOOP 5
 int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value);
 int nli_ctx_get_tuning(nli_ctx *ctx, int knob, int *value);
 /* The seed image `index` of a batch runs with. */

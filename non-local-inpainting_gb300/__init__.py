@@ -481,7 +481,7 @@ class Context:
         self._check(rc)
         return outs, [s.as_dict() for s in st]
 
-    TUNE_CG_CLUSTER_CAP, TUNE_CG_UNKNOWNS_PER_CTA, TUNE_BATCH_WIDTH, TUNE_PM_VARIANT, TUNE_CG_PRECOND = 0, 1, 2, 3, 4
+    TUNE_CG_CLUSTER_CAP, TUNE_CG_UNKNOWNS_PER_CTA, TUNE_BATCH_WIDTH, TUNE_PM_VARIANT, TUNE_CG_PRECOND, TUNE_GRAPH_LOOP = 0, 1, 2, 3, 4, 5
 
     def set_tuning(self, knob, value):
         self._check(self.lib.nli_ctx_set_tuning(self.h, knob, value))

@@ -60,7 +60,8 @@ class ProcessStats(ct.Structure):
                 ("iterations", ct.c_int32 * NLI_MAX_SCALES),
                 ("last_difference", ct.c_double * NLI_MAX_SCALES),
                 ("patchmatch_calls", ct.c_int64), ("update_calls", ct.c_int64),
-                ("cg_iterations", ct.c_int64), ("candidates", ct.c_int64)]
+                ("cg_iterations", ct.c_int64), ("candidates", ct.c_int64),
+                ("graph_iterations", ct.c_int64)]
 
     def as_dict(self):
         n = self.scales
@@ -68,7 +69,8 @@ class ProcessStats(ct.Structure):
                 "iterations": list(self.iterations[:n]),
                 "last_difference": list(self.last_difference[:n]),
                 "patchmatch_calls": self.patchmatch_calls, "update_calls": self.update_calls,
-                "cg_iterations": self.cg_iterations, "candidates": self.candidates}
+                "cg_iterations": self.cg_iterations, "candidates": self.candidates,
+                "graph_iterations": self.graph_iterations}
 
 
 _libm = None

@@ -193,7 +193,11 @@ int nli_set_seed(nli_ctx *ctx, uint64_t seed)
 {
 	if (!ctx) return NLI_E_INVALID;
 	ctx->seed = seed;
-	ctx->call_counter = 0;
+	try {
+		NLI_CUDA(cudaMemsetAsync(&ctx->status->pm_calls, 0, sizeof(unsigned long long), ctx->stream));
+	} catch (const Error &e) {
+		return fail(ctx, e);
+	}
 	return NLI_OK;
 }
 
@@ -207,8 +211,21 @@ int nli_ctx_synchronize(nli_ctx *ctx)
 const char *nli_last_error(nli_ctx *ctx) { return ctx ? ctx->last_error.c_str() : "null context"; }
 
 static std::atomic<long long> g_launches{0};
+static thread_local long long t_launches = 0;
 
-void nli_count_launch_internal(void) { g_launches.fetch_add(1, std::memory_order_relaxed); }
+void nli_count_launch_internal(void)
+{
+	g_launches.fetch_add(1, std::memory_order_relaxed);
+	t_launches++;
+}
+
+long long nli_thread_launch_count_internal(void) { return t_launches; }
+
+void nli_add_launches_internal(long long n)
+{
+	g_launches.fetch_add(n, std::memory_order_relaxed);
+	t_launches += n;
+}
 
 int64_t nli_launch_count(void) { return g_launches.load(); }
 
@@ -598,6 +615,10 @@ int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value)
 		if (value != 0 && value != 1) return NLI_E_INVALID;
 		ctx->tune_cg_precond = value;
 		return NLI_OK;
+	case NLI_TUNE_GRAPH_LOOP:
+		if (value < 0 || value > 2) return NLI_E_INVALID;
+		ctx->tune_graph_loop = value;
+		return NLI_OK;
 	}
 	return NLI_E_INVALID;
 }
@@ -611,6 +632,7 @@ int nli_ctx_get_tuning(nli_ctx *ctx, int knob, int *value)
 	case NLI_TUNE_BATCH_WIDTH: *value = ctx->batch_width; return NLI_OK;
 	case NLI_TUNE_PM_VARIANT: *value = ctx->tune_pm_variant; return NLI_OK;
 	case NLI_TUNE_CG_PRECOND: *value = ctx->tune_cg_precond; return NLI_OK;
+	case NLI_TUNE_GRAPH_LOOP: *value = ctx->tune_graph_loop; return NLI_OK;
 	}
 	return NLI_E_INVALID;
 }

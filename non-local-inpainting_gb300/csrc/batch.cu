@@ -32,6 +32,7 @@ static nli_ctx *new_worker(int device)
 	nli_ctx *w = nullptr;
 	const int rc = nli_ctx_create(device, &w);
 	NLI_REQUIRE(rc == NLI_OK, rc, "cannot create a batch worker context");
+	w->batch_worker = true;
 	return w;
 }
 
@@ -84,6 +85,7 @@ void process_batch_run(nli_ctx *ctx, int n, const nli_process_params *params, co
 		w->tune_cg_unknowns_per_cta = ctx->tune_cg_unknowns_per_cta;
 		w->tune_pm_variant = ctx->tune_pm_variant;
 		w->tune_cg_precond = ctx->tune_cg_precond;
+		w->tune_graph_loop = ctx->tune_graph_loop;
 		if (ready) cudaStreamWaitEvent(w->stream, ready, 0);
 		for (;;) {
 			const int k = next.fetch_add(1);
@@ -99,7 +101,7 @@ void process_batch_run(nli_ctx *ctx, int n, const nli_process_params *params, co
 				std::snprintf(label, sizeof(label), "batch image %d", i);
 				NvtxRange image_range(label);
 				w->seed = batch_seed(ctx->seed, i);
-				w->call_counter = 0;
+				NLI_CUDA(cudaMemsetAsync(&w->status->pm_calls, 0, sizeof(unsigned long long), w->stream));
 				nli_process_stats *st = stats ? stats + i : nullptr;
 				if (host_buffers) {
 					const size_t np = (size_t)W * H;

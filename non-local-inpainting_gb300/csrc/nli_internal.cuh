@@ -32,8 +32,12 @@ struct Error {
 	} while (0)
 
 // Every kernel launch of the library is followed by this check, which also
-// counts the launch (nli_launch_count).
+// counts the launch (nli_launch_count).  The calling thread's own count
+// tells a graph capture how many launches its body holds; replays of a
+// captured body are added with nli_add_launches_internal.
 extern "C" void nli_count_launch_internal(void);
+extern "C" long long nli_thread_launch_count_internal(void);
+extern "C" void nli_add_launches_internal(long long n);
 #define NLI_CHECK_LAUNCH()                    \
 	do {                                      \
 		nli_count_launch_internal();          \
@@ -71,12 +75,16 @@ struct DevBuf {
 	}
 };
 
-// Device-side status words written by kernels that wait (grid barriers).
+// Device-side status words written by kernels that wait (grid barriers),
+// and the index of the context's PatchMatch calls since its seed was set
+// (kept on the device so that a captured iteration loop draws the same
+// random streams as launches from the host).
 struct DevStatus {
 	unsigned int barrier_count;
 	unsigned int barrier_gen;
 	int timeout;
 	int pad;
+	unsigned long long pm_calls;
 };
 
 }  // namespace nli
@@ -86,7 +94,6 @@ struct nli_ctx {
 	cudaStream_t own_stream = nullptr;
 	cudaStream_t stream = nullptr;
 	uint64_t seed = 0x9e3779b97f4a7c15ULL;
-	uint64_t call_counter = 0;
 	std::string last_error;
 	int num_sms = 0;
 	int cg_cluster_max = -1;  // largest thread-block cluster for the CG kernel (queried once)
@@ -123,6 +130,9 @@ struct nli_ctx {
 	int tune_cg_unknowns_per_cta = 1024; // at least this many unknowns per CG CTA
 	int tune_pm_variant = 0;             // 9x9 PatchMatch window reads (PmVariant)
 	int tune_cg_precond = 0;             // NL-Poisson CG: 0 plain (the reference's), 1 Jacobi
+	int tune_graph_loop = 1;             // iterations 1.. of a scale as one CUDA graph (while node):
+	                                     // 1 in nli_process only, 2 also in batches, 0 never
+	bool batch_worker = false;           // a worker context of nli_process_batch
 	int max_smem_optin = 0;              // dynamic shared memory per block at most
 	std::vector<nli_ctx *> workers;
 	std::vector<cudaEvent_t> event_pool;
@@ -252,10 +262,13 @@ void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patch
                     int n_target = -1, PatchMatchMetricsHost *metrics = nullptr);
 
 // update.cu
+// read_back false: nothing is read to the host; *total_dev (if given)
+// receives the device address of the step's sum (du)^2 and *cg_iters_dev
+// that of the per-channel CG iteration counts (null for NL-means/medians).
 double update_run(nli_ctx *ctx, const nli_update_params &up, float *image, const float *orig,
                   const uint8_t *dom, const uint8_t *ext, const int32_t *nnf, const float *conf, int W,
                   int H, int C, const int32_t *hole_list = nullptr, int n_hole = -1,
-                  bool read_back = true);
+                  bool read_back = true, const double **total_dev = nullptr, const int **cg_iters_dev = nullptr);
 
 // Adjoint of one update with the NNF fixed (update.cu).
 void update_backward_run(nli_ctx *ctx, const nli_update_params &up, const float *image, const float *out,

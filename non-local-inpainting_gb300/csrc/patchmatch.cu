@@ -129,13 +129,23 @@ struct PmArgs {
 	int sW, sH, tW, tH, nt;
 	int sWp, tWp;
 	int shots, max_window;
-	uint2 key;
+	uint64_t seed;                     // the context's seed
+	const unsigned long long *calls;   // PatchMatch calls so far, this one included
 	// patch extent around a centre: [x - rx, x + ex) x [y - ry, y + ey)
 	int rx, ry, ex, ey;
 	// lanes per candidate, candidates per warp step, window rows
 	int L, K, rows;
 	float lambda, lambda_d;
 };
+
+// Philox key of this PatchMatch call: the seed mixed with the call's index
+// (0 for the first call after the seed is set).
+__device__ __forceinline__ uint2 pm_key(const PmArgs &p)
+{
+	const uint64_t call = *p.calls - 1ull;
+	const uint64_t k = p.seed ^ (call * 0x9E3779B97F4A7C15ULL);
+	return make_uint2((uint32_t)k, (uint32_t)(k >> 32) ^ (uint32_t)call);
+}
 
 template <int KIND>
 struct Kind {
@@ -555,6 +565,7 @@ __global__ void __launch_bounds__(pm_threads(V), 1) k_pm_init(DistArgs a, PmArgs
 	if (V == kPmStaged && lane == 0) mbar_init(m.bar, 1);
 	float4 tw[(V == kPmRegs) ? P + 1 : 1];
 	load_weights(a, m.w);
+	const uint2 key = pm_key(p);
 	unsigned evals = 0, partial = 0;
 	// block b takes the contiguous range [b * chunk, (b + 1) * chunk) of the
 	// raster-ordered target list, its warps interleaved over the range, so
@@ -565,7 +576,7 @@ __global__ void __launch_bounds__(pm_threads(V), 1) k_pm_init(DistArgs a, PmArgs
 	for (int wi = blockIdx.x * chunk + (threadIdx.x >> 5); wi < end; wi += blockDim.x >> 5) {
 		const int pix = p.tlist[wi];
 		const int x = pix % p.tW, y = pix / p.tW;
-		Rng rng(p.key, (uint32_t)pix, 0xffffffffu);
+		Rng rng(key, (uint32_t)pix, 0xffffffffu);
 		int2 n = init ? init[pix] : make_int2(-1, -1);
 		int tries = 0;
 		// patch_match.cpp:341-381: keep a seed match that lies in the
@@ -622,6 +633,7 @@ __global__ void __launch_bounds__(pm_threads(V), 1) k_pm_sweep(DistArgs a, PmArg
 	if (V == kPmStaged && lane == 0) mbar_init(m.bar, 1);
 	float4 tw[(V == kPmRegs) ? P + 1 : 1];
 	load_weights(a, m.w);
+	const uint2 key = pm_key(p);
 	unsigned evals = 0, partial = 0, improved = 0;
 	int max_shot = -1;
 	// number of random-search windows: max_window, max_window / 2, ..., 1
@@ -670,7 +682,7 @@ __global__ void __launch_bounds__(pm_threads(V), 1) k_pm_sweep(DistArgs a, PmArg
 				const int w = p.max_window >> lane;
 				const int x_min = max(best.x - w, 0), y_min = max(best.y - w, 0);
 				const int x_max = min(best.x + w + 1, p.sW), y_max = min(best.y + w + 1, p.sH);
-				Rng rng(p.key, (uint32_t)pix, (uint32_t)sweep, (uint32_t)lane);
+				Rng rng(key, (uint32_t)pix, (uint32_t)sweep, (uint32_t)lane);
 #pragma unroll 1
 				for (int t = 0; t < p.shots; t++) {
 					const int rx = x_min + rng.below(x_max - x_min);
@@ -707,8 +719,10 @@ __global__ void __launch_bounds__(pm_threads(V), 1) k_pm_sweep(DistArgs a, PmArg
 	}
 }
 
-__global__ void k_fill_nnf(int2 *__restrict__ nnf, float *__restrict__ dist, int n)
+// Also advances the context's PatchMatch call index when `calls` is set.
+__global__ void k_fill_nnf(int2 *__restrict__ nnf, float *__restrict__ dist, int n, unsigned long long *calls)
 {
+	if (calls && blockIdx.x == 0 && threadIdx.x == 0) *calls += 1ull;
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
 		nnf[i] = make_int2(-1, -1);
 		if (dist) dist[i] = FLT_MAX;
@@ -900,7 +914,9 @@ void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patch
 	float *dist_y = ctx->buf<float>("pm.dist_y", nT);
 	// [0]: candidates evaluated, [1]: of these, stopped after the first 32 taps
 	unsigned long long *counter = ctx->buf<unsigned long long>("pm.counter", 2);
-	k_fill_nnf<<<(nT + 255) / 256, 256, 0, s>>>(nnf_x, out_dist, nT);
+	// the call index advances only for calls with target points, as the
+	// random streams are drawn only then
+	k_fill_nnf<<<(nT + 255) / 256, 256, 0, s>>>(nnf_x, out_dist, nT, n_target > 0 ? &ctx->status->pm_calls : nullptr);
 	NLI_CHECK_LAUNCH();
 	if (n_target > 0) {
 		PmArgs p;
@@ -928,9 +944,8 @@ void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patch
 		p.rows = a.py + (grad ? 1 : 0);
 		p.lambda = a.lambda;
 		p.lambda_d = a.lambda_d;
-		const uint64_t call = ctx->call_counter++;
-		const uint64_t k = ctx->seed ^ (call * 0x9E3779B97F4A7C15ULL);
-		p.key = make_uint2((uint32_t)k, (uint32_t)(k >> 32) ^ (uint32_t)call);
+		p.seed = ctx->seed;
+		p.calls = &ctx->status->pm_calls;  // advanced by k_fill_nnf above
 		if (energy) NLI_CUDA(cudaMemsetAsync(counter, 0, 2 * sizeof(unsigned long long), s));
 		PmMetrics mt;
 		const int iters = std::max(pm.iterations, 0);

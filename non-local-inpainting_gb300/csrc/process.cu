@@ -96,13 +96,41 @@ __global__ void k_fill_int2(int2 *p, int n, int2 v)
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = v;
 }
 
+// Device state of a captured iteration loop: iterations done on the level,
+// the last sum (du)^2, and the CG iteration counts the host loop would have
+// read after each update.
+struct LoopState {
+	int iter;
+	int pad;
+	double total;
+	long long cg_iters, cg_unknown_iters;
+};
+
+// End of one captured iteration: the stopping test of inpaint_internal
+// (image_inpainting.cpp:388-408: continue while iter < iterations and
+// total > tolerance) decides whether the graph's while node runs again.
+__global__ void k_loop_control(cudaGraphConditionalHandle h, LoopState *st, const double *total, const int *cg_iters,
+                               int C, int nh, int iterations, double tolerance)
+{
+	const int i = st->iter + 1;
+	st->iter = i;
+	const double t = *total;
+	st->total = t;
+	if (cg_iters)
+		for (int c = 0; c < C; c++) {
+			st->cg_iters += cg_iters[c];
+			st->cg_unknown_iters += (long long)cg_iters[c] * nh;
+		}
+	cudaGraphSetConditional(h, (i < iterations && t > tolerance) ? 1u : 0u);
+}
+
 struct Driver {
 	nli_ctx *ctx;
 	const nli_process_params &p;
 	int C;
 	std::vector<Level> lv;
 	nli_process_stats *stats;
-	int64_t pm_calls = 0, upd_calls = 0;
+	int64_t pm_calls = 0, upd_calls = 0, graph_iters = 0;
 
 	Driver(nli_ctx *c, const nli_process_params &pp, int CC, nli_process_stats *st) : ctx(c), p(pp), C(CC), stats(st) {}
 
@@ -178,7 +206,18 @@ struct Driver {
 		char label[64];
 		std::snprintf(label, sizeof(label), "scale %d (%dx%d)", l, L.W, L.H);
 		NvtxRange scale_range(label);
+		// with the captured loop, iteration 0 runs from the host (it sizes
+		// every buffer the graph then reuses) and the rest in one graph
+		const bool graph =
+		    (ctx->tune_graph_loop == 2 || (ctx->tune_graph_loop == 1 && !ctx->batch_worker)) && !ctx->profiling &&
+		    L.nh > 0;
 		for (i = 0; i < p.iterations && total > p.tolerance; i++) {
+			if (graph && i == 1) {
+				// iteration 0 left the field in one of the two buffers
+				int32_t *field = const_cast<int32_t *>(nnf);
+				int32_t *other = (field == bufs[0]) ? bufs[1] : bufs[0];
+				if (graph_loop(L, orig, other, field, i, total)) break;
+			}
 			NvtxRange iteration_range("iteration");
 			int32_t *out = (nnf == bufs[cur]) ? bufs[1 - cur] : bufs[cur];
 			pm(L.img, L.src_eroded, L, nnf, out);
@@ -192,6 +231,107 @@ struct Driver {
 		}
 		if (ctx->keep_intermediate) ctx->inter_nnf.push_back(keep(ctx, nnf, L.W, L.H, 2, sizeof(int32_t)));
 		return const_cast<int32_t *>(nnf);
+	}
+
+	// Iterations i.. of a level as one CUDA graph: a while node whose body is
+	// PatchMatch (A -> B), the update with B, B copied back to A and
+	// k_loop_control, which evaluates the stopping test on the device.  The
+	// field enters in B (after iteration i - 1) and leaves in B.  Returns
+	// false, with nothing run, when the loop cannot be captured; the caller
+	// then goes on from the host.  On return `i` and `total` are as the host
+	// loop would leave them.
+	bool graph_loop(Level &L, const float *orig, int32_t *A, int32_t *B, int &i, double &total)
+	{
+		// The body is captured on the context's own stream (capture is not
+		// possible on the legacy default stream a caller may have set) and
+		// the graph is launched on the context's current stream.
+		cudaStream_t s = ctx->stream;
+		cudaStream_t cap = ctx->own_stream ? ctx->own_stream : s;
+		const size_t n = (size_t)L.W * L.H;
+		LoopState *st = ctx->buf<LoopState>("proc.loop", 1);
+		cudaGraph_t g = nullptr;
+		cudaGraphExec_t ex = nullptr;
+		const int64_t pm0 = pm_calls, up0 = upd_calls;
+		const int64_t launches0 = nli_thread_launch_count_internal();
+		bool capturing = false;
+		try {
+			NLI_CUDA(cudaGraphCreate(&g, 0));
+			cudaGraphConditionalHandle h;
+			NLI_CUDA(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+			cudaGraphNodeParams cp = {};
+			cp.type = cudaGraphNodeTypeConditional;
+			cp.conditional.handle = h;
+			cp.conditional.type = cudaGraphCondTypeWhile;
+			cp.conditional.size = 1;
+			cudaGraphNode_t node;
+			NLI_CUDA(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp));
+			cudaGraph_t body = cp.conditional.phGraph_out[0];
+			NLI_CUDA(cudaStreamBeginCaptureToGraph(cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+			capturing = true;
+			ctx->stream = cap;
+			pm(L.img, L.src_eroded, L, A, B);
+			const double *tdev = nullptr;
+			const int *cgdev = nullptr;
+			upd_calls++;
+			update_run(ctx, p.update, L.img, orig, L.mask, L.ext, B, L.conf, L.W, L.H, C, L.hole, L.nh, false, &tdev,
+			           &cgdev);
+			NLI_REQUIRE(tdev != nullptr, NLI_E_UNSUPPORTED, "no device total to test");
+			NLI_CUDA(cudaMemcpyAsync(A, B, 2 * n * sizeof(int32_t), cudaMemcpyDeviceToDevice, cap));
+			k_loop_control<<<1, 1, 0, cap>>>(h, st, tdev, cgdev, C, L.nh, p.iterations, (double)p.tolerance);
+			NLI_CHECK_LAUNCH();
+			capturing = false;
+			ctx->stream = s;
+			NLI_CUDA(cudaStreamEndCapture(cap, &body));
+			NLI_CUDA(cudaGraphInstantiate(&ex, g, 0));
+		} catch (const Error &) {
+			ctx->stream = s;
+			if (capturing) {
+				cudaGraph_t dummy = nullptr;
+				cudaStreamEndCapture(cap, &dummy);
+			}
+			(void)cudaGetLastError();
+			if (ex) cudaGraphExecDestroy(ex);
+			if (g) cudaGraphDestroy(g);
+			pm_calls = pm0;
+			upd_calls = up0;
+			nli_add_launches_internal(launches0 - nli_thread_launch_count_internal());  // nothing ran
+			return false;
+		}
+		const int64_t body_launches = nli_thread_launch_count_internal() - launches0;
+		// the field to A, the loop state, then the graph
+		LoopState init = {i, 0, total, 0, 0};
+		LoopState *hs = static_cast<LoopState *>(ctx->host_pinned);
+		*hs = init;
+		try {
+			NLI_CUDA(cudaMemcpyAsync(A, B, 2 * n * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+			NLI_CUDA(cudaMemcpyAsync(st, hs, sizeof(LoopState), cudaMemcpyHostToDevice, s));
+			NLI_CUDA(cudaGraphLaunch(ex, s));
+			NLI_CUDA(cudaMemcpyAsync(hs, st, sizeof(LoopState), cudaMemcpyDeviceToHost, s));
+			NLI_CUDA(cudaMemcpyAsync(reinterpret_cast<char *>(hs) + 64, &ctx->status->timeout, sizeof(int),
+			                         cudaMemcpyDeviceToHost, s));
+			NLI_CUDA(cudaStreamSynchronize(s));
+		} catch (const Error &) {
+			cudaGraphExecDestroy(ex);
+			cudaGraphDestroy(g);
+			throw;
+		}
+		cudaGraphExecDestroy(ex);
+		cudaGraphDestroy(g);
+		const int ran = hs->iter - i;
+		// the host counters as the host loop would have left them
+		pm_calls = pm0 + ran;
+		upd_calls = up0 + ran;
+		graph_iters += ran;
+		nli_add_launches_internal(body_launches * (ran - 1));
+		ctx->cg_iterations += hs->cg_iters;
+		ctx->cg_unknown_iterations += hs->cg_unknown_iters;
+		i = hs->iter;
+		total = hs->total;
+		if (*reinterpret_cast<const int *>(reinterpret_cast<char *>(hs) + 64) != 0) {
+			clear_timeout(ctx);
+			NLI_REQUIRE(false, NLI_E_TIMEOUT, "a device-side wait timed out");
+		}
+		return true;
 	}
 
 	// propagate_weights: returns the refined NNF of level l (the finer one)
@@ -314,6 +454,7 @@ struct Driver {
 			stats->patchmatch_calls = pm_calls;
 			stats->update_calls = upd_calls;
 			stats->cg_iterations = ctx->cg_iterations - cg0;
+			stats->graph_iterations = graph_iters;
 			stats->candidates = (int64_t)hc[0];
 		}
 	}

@@ -1184,8 +1184,19 @@ static int poisson_solve(nli_ctx *ctx, PoissonSystem &P, const int32_t *hole, co
 	void *args[] = {&P.pa, &unk, &b,   &x,     (void *)&r, &d, &q, &z, &part, &st, &iters, (void *)&hole,
 	                &orig, &img, &diff_part};
 	{
+		// cooperative through the launch attribute, which stream capture takes
+		cudaLaunchConfig_t cfg = {};
+		cfg.gridDim = dim3(grid);
+		cfg.blockDim = dim3(kCgBlock);
+		cfg.dynamicSmemBytes = 0;
+		cfg.stream = s;
+		cudaLaunchAttribute attr[1];
+		attr[0].id = cudaLaunchAttributeCooperative;
+		attr[0].val.cooperative = 1;
+		cfg.attrs = attr;
+		cfg.numAttrs = 1;
 		ProfScope ps(ctx, "poisson_cg");
-		NLI_CUDA(cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(kCgBlock), args, 0, s));
+		NLI_CUDA(cudaLaunchKernelExC(&cfg, kern, args));
 		nli_count_launch_internal();
 	}
 	return grid;
@@ -1201,7 +1212,7 @@ static void poisson_run(nli_ctx *ctx, const UpdArgs &u, const nli_update_params 
 
 double update_run(nli_ctx *ctx, const nli_update_params &up, float *image, const float *orig, const uint8_t *dom,
                   const uint8_t *ext, const int32_t *nnf_i, const float *conf, int W, int H, int C,
-                  const int32_t *hole, int nh, bool read_back)
+                  const int32_t *hole, int nh, bool read_back, const double **total_dev, const int **cg_iters_dev)
 {
 	NLI_REQUIRE(up.method >= 0 && up.method <= 3, NLI_E_UNSUPPORTED, "unknown update method");
 	if (up.method == NLI_UPDATE_DEPTH) NLI_REQUIRE(C == 4, NLI_E_CHANNELS, "Separate: Channels do not match.");
@@ -1228,6 +1239,8 @@ double update_run(nli_ctx *ctx, const nli_update_params &up, float *image, const
 		double *diff_part = ctx->buf<double>("poi.diff", np + 1);
 		if (!read_back) {
 			launch_sum_partials(s, diff_part, np, diff_part + np);
+			if (total_dev) *total_dev = diff_part + np;
+			if (cg_iters_dev) *cg_iters_dev = ctx->buf<int>("poi.iters", 4);
 			return 0.0;
 		}
 		return read_total(ctx, diff_part, np, ctx->buf<int>("poi.iters", 4), C, nh);
@@ -1251,6 +1264,8 @@ double update_run(nli_ctx *ctx, const nli_update_params &up, float *image, const
 	NLI_CHECK_LAUNCH();
 	if (!read_back) {
 		launch_sum_partials(s, partials, grid, partials + grid);
+		if (total_dev) *total_dev = partials + grid;
+		if (cg_iters_dev) *cg_iters_dev = nullptr;
 		return 0.0;
 	}
 	return read_total(ctx, partials, grid, nullptr, C);
