@@ -41,8 +41,23 @@ import __graft_entry__ as ge  # noqa: E402
 METRIC = "inpainted Mpix/s on 1 GB300, batched vs plain GPU path, ≤0.1 dB PSNR gap to ref"
 UNIT = "Mpix/s"
 # algorithmic FP32 work of one patch distance, P = 9: 31 P^2 + 8 (C = 3,
-# L2Combined: 9 differences, 9 squares/FMAs and 2 weighted FMAs per tap)
+# L2Combined: 9 differences, 9 squares/FMAs and 2 weighted FMAs per tap);
+# 44 P^2 + 8 for the 4-channel L2 RGBD distance
 FLOP_PER_CANDIDATE = 31 * 81 + 8
+FLOP_PER_CANDIDATE_RGBD = 44 * 81 + 8
+# the workload of the run (--workload); the headline is the 512x512 NL-Poisson one
+WORKLOAD = "nlpoisson512"
+WORKLOADS = {
+    "nlpoisson512": ("512x512 RGB float32 Voronoi (40 seeds) + oriented sinusoids, union of 6 ellipses (~15% hole); "
+                     "nlpoisson + L2Combined, lambda 0.05, psigma 10000, patch 9, scales 8, coarse 0.1, CG tol 1e-4, "
+                     "iters 200, tol 0.1, conft 5, confa 0.1, init poisson, PatchMatch 10 sweeps / 30 shots"),
+    "nlmeans256": ("256x256 RGB float32 smooth gradient + stripes (period 12) + noise (sigma 3), centred disc of "
+                   "radius 32 (~4.9% hole); nlmeans + L2Combined, lambda 0.05, psigma 10000, patch 9, scales 5, "
+                   "coarse 0.1, iters 200, tol 0.1, conft 5, confa 0.1, init poisson, PatchMatch 10 sweeps / 30 shots"),
+    "nldepth640": ("640x480 RGB-D float32 Voronoi (60 seeds) + depth of 3-8 planes in [0.5, 5] m, 10 brush strokes "
+                   "(~12% hole); nldepth + L2RGBD, lambda_rgb 1.0, lambda_d 0.0, psigma 10000, patch 9, scales 9, "
+                   "coarse 0.1, iters 200, tol 0.1, conft 5, confa 0.1, init poisson, PatchMatch 10 sweeps / 30 shots"),
+}
 # algorithmic bytes of one CG iteration per unknown and channel: read d, a1,
 # a2-links, x, r, q; write x, r, d (float32), as counted for the roofline
 CG_BYTES_PER_UNKNOWN_ITER = 32
@@ -55,15 +70,21 @@ TRAFFIC = os.path.join(ROOT, "profiles", "pm_sweep_l2combined_512x512.md")
 
 
 def workload_desc():
-    return ("512x512 RGB float32 Voronoi (40 seeds) + oriented sinusoids, union of 6 ellipses (~15% hole); "
-            "nlpoisson + L2Combined, lambda 0.05, psigma 10000, patch 9, scales 8, coarse 0.1, CG tol 1e-4, "
-            "iters 200, tol 0.1, conft 5, confa 0.1, init poisson, PatchMatch 10 sweeps / 30 shots")
+    return WORKLOADS[WORKLOAD]
 
 
 def workload(seed=0):
-    pkg = ge.package()
+    ge.package()
     from nli_gb300 import workloads as wl
+    if WORKLOAD == "nlmeans256":
+        return wl.config1(seed=seed)
+    if WORKLOAD == "nldepth640":
+        return wl.config3(seed=seed)
     return wl.config2(seed=seed)
+
+
+def flop_per_candidate():
+    return FLOP_PER_CANDIDATE_RGBD if WORKLOAD == "nldepth640" else FLOP_PER_CANDIDATE
 
 
 class Clocks:
@@ -113,8 +134,9 @@ class Clocks:
 
 def reference_counts():
     """Per-scale PatchMatch / update call counts of the reference on this
-    workload (serial run, committed fixture), finest scale first."""
-    if os.path.exists(COUNTS):
+    workload (serial run, committed fixture), finest scale first; the
+    fixture covers the 512x512 NL-Poisson workload."""
+    if WORKLOAD == "nlpoisson512" and os.path.exists(COUNTS):
         with open(COUNTS) as f:
             c = json.load(f)
         return c["iterations"], "reference run (seed %d)" % c.get("seed", 0)
@@ -342,18 +364,18 @@ def run_ours(args):
     pm_ms = sum(v[1] for k, v in prof.items() if k.startswith("pm_"))
     pm_launches = sum(v[0] for k, v in prof.items() if k.startswith("pm_"))
     traffic = None
-    if os.path.exists(TRAFFIC):
+    if WORKLOAD == "nlpoisson512" and os.path.exists(TRAFFIC):
         import re
         m = re.search(r"traffic_bytes_per_launch:\s*(\d+)", open(TRAFFIC).read())
         traffic = int(m.group(1)) if m else None
-    pm_tflops = cand * FLOP_PER_CANDIDATE / (pm_ms / 1e3) / 1e12 if pm_ms > 0 else 0.0
+    pm_tflops = cand * flop_per_candidate() / (pm_ms / 1e3) / 1e12 if pm_ms > 0 else 0.0
     roofline = {"kernel": "k_pm_init + k_pm_sweep (PatchMatch)", "bound": "fp32", "achieved": pm_tflops,
                 "peak": fp32_peak, "unit": "TFLOP/s", "frac": pm_tflops / fp32_peak if fp32_peak else None,
                 "traffic": traffic, "traffic_scope": "ncu DRAM bytes of one finest-scale (512x512) sweep launch",
                 "launches": pm_launches, "ms": pm_ms,
                 "peak_source": "nominal FP32 (%d SMs x 128 lanes x 2 FLOP) at the sampled median SM clock %.0f MHz; "
                                "MEASURED_PEAKS.json has no FP32 figure" % (n_sm, sm_mhz),
-                "flop_per_candidate": FLOP_PER_CANDIDATE, "candidates": cand}
+                "flop_per_candidate": flop_per_candidate(), "candidates": cand}
     cg = prof.get("poisson_cg", (0, 0.0))
     cg_work = c1["cg_unknown_iterations"] - c0["cg_unknown_iterations"]
     cg_gbs = cg_work * CG_BYTES_PER_UNKNOWN_ITER / (cg[1] / 1e3) / 1e9 if cg[1] > 0 else 0.0
@@ -363,11 +385,13 @@ def run_ours(args):
     if world == 1 and not args.no_cpu_baseline:
         iters, source = reference_counts()
         if iters is None:
-            iters, source = list(st.iterations[:p.scales]), "GPU run (reference counts missing)"
+            iters, source = list(st.iterations[:p.scales]), "GPU run (no reference counts for this workload)"
         est, wall, threads = cpu_sample(img, mask, p, iters)
+        method = {0: "NL-means", 1: "NL-medians", 2: "NL-Poisson", 3: "NL-depth"}.get(p.update.method, "update")
         cpu = {"value": mpix / est, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": "1 PatchMatch (OpenMP) + 1 NL-Poisson update on each of the 8 scales (%.1f s wall), scaled "
-                         "by the per-scale call counts of the %s: %.1f s per process()" % (wall, source, est)}
+               "sample": "1 PatchMatch (OpenMP) + 1 %s update on each of the %d scales (%.1f s wall), scaled "
+                         "by the per-scale call counts of the %s: %.1f s per process()"
+                         % (method, p.scales, wall, source, est)}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -520,6 +544,8 @@ def main():
                     help="9x9 PatchMatch window reads: 0 target in shared memory + plain source loads, "
                          "1 source windows staged by tensor copies, 2 target in registers "
                          "(default: the library's)")
+    ap.add_argument("--workload", default="nlpoisson512", choices=sorted(WORKLOADS),
+                    help="nlpoisson512 (the headline, default), nlmeans256 or nldepth640")
     ap.add_argument("--no-variants", action="store_true",
                     help="skip the extra measurement with the Jacobi-preconditioned CG")
     ap.add_argument("--cg-precond", type=int, default=None, choices=[0, 1],
@@ -532,6 +558,8 @@ def main():
     ap.add_argument("--no-batch-profile", dest="batch_profile", action="store_false",
                     help="skip the per-kernel profiled passes of the batch comparison")
     args = ap.parse_args()
+    global WORKLOAD
+    WORKLOAD = args.workload
     if args.case:
         return run_case(args)
     if args.impl == "reference":
