@@ -1,0 +1,71 @@
+"""Host-side logic that needs no GPU: the autotuner's cache file and
+re-application (against a recording stand-in for the context), the
+benchmark's workload table and throughput arithmetic, and the ABI's tuning
+constants as the Python binding and the C header declare them."""
+import json
+import os
+import re
+
+import pytest
+
+import bench
+from nli_gb300 import autotune
+
+
+class FakeCtx:
+    """Records what autotune.apply sets; the knob numbers are the binding's."""
+
+    def __init__(self):
+        import nli_gb300 as pkg
+        for k in ("TUNE_CG_CLUSTER_CAP", "TUNE_CG_UNKNOWNS_PER_CTA", "TUNE_BATCH_WIDTH", "TUNE_PM_VARIANT",
+                  "TUNE_CG_PRECOND", "TUNE_GRAPH_LOOP"):
+            setattr(self, k, getattr(pkg.Context, k))
+        self.tuning = {}
+        self.batch_width = None
+
+    def set_tuning(self, knob, value):
+        self.tuning[knob] = value
+
+    def set_batch_width(self, width):
+        self.batch_width = width
+
+
+def test_cache_round_trip_on_host(tmp_path):
+    path = str(tmp_path / "tuning.json")
+    ctx = FakeCtx()
+    assert autotune.load(ctx, path, "dev") is None
+    autotune.save(path, "dev", cg=(12, 2048), batch_width=6, pm_variant=2)
+    autotune.save(path, "other", cg=(4, 512))
+    assert autotune.load(ctx, path, "missing") is None
+    got = autotune.load(ctx, path, "dev")
+    assert got == {"cg": [12, 2048], "batch_width": 6, "pm_variant": 2}
+    assert ctx.tuning == {ctx.TUNE_CG_CLUSTER_CAP: 12, ctx.TUNE_CG_UNKNOWNS_PER_CTA: 2048, ctx.TUNE_PM_VARIANT: 2}
+    assert ctx.batch_width == 6
+    with open(path) as f:
+        table = json.load(f)
+    assert set(table) == {"dev", "other"} and table["other"] == {"cg": [4, 512]}
+    assert not os.path.exists(path + ".tmp")
+
+
+def test_tuning_constants_match_the_header():
+    """The binding's TUNE_* numbers are the header's NLI_TUNE_* defines."""
+    import nli_gb300 as pkg
+    here = os.path.dirname(os.path.abspath(__file__))
+    header = open(os.path.join(here, "..", "include", "nli.h")).read()
+    defines = dict((m.group(1), int(m.group(2))) for m in re.finditer(r"#define NLI_(TUNE_\w+) (\d+)", header))
+    assert len(defines) == 6
+    for name, value in defines.items():
+        assert getattr(pkg.Context, name) == value, name
+
+
+def test_bench_workloads_and_throughput():
+    assert set(bench.WORKLOADS) == {"nlpoisson512", "nlmeans256", "nldepth640"}
+    for name in bench.WORKLOADS:
+        bench.WORKLOAD = name
+        try:
+            assert bench.workload_desc() == bench.WORKLOADS[name]
+            assert bench.flop_per_candidate() == (44 * 81 + 8 if name == "nldepth640" else 31 * 81 + 8)
+        finally:
+            bench.WORKLOAD = "nlpoisson512"
+    # whole-job throughput: N ranks x steps x Mpix per rank and step / seconds
+    assert bench.job_throughput(2, 5, 0.262144, 1000.0) == pytest.approx(2 * 5 * 0.262144)
