@@ -89,12 +89,14 @@ CLI = os.path.join(HERE, "nli_inpaint")
 def build_cli(force=False):
     """nli_inpaint: the reference's command-line program over the drop-in classes."""
     src = os.path.join(CSRC, "cli.cpp")
-    deps = [src, LIB, DROPIN, os.path.join(ROOT, "include", "nli_inpainting.hpp"), os.path.join(ROOT, "include", "nli.h")]
+    png = [os.path.join(CSRC, "png_codec.cpp"), os.path.join(CSRC, "png_codec.h")]
+    deps = [src, LIB, DROPIN, os.path.join(ROOT, "include", "nli_inpainting.hpp"),
+            os.path.join(ROOT, "include", "nli.h")] + png
     if not force and not _stale(CLI, deps):
         return CLI
     _run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), "-I", os.path.join(CUDA_HOME, "include"),
-          src, "-o", CLI + ".tmp", "-L", HERE, "-lnli_dropin", "-lnli_gb300", "-L", os.path.join(CUDA_HOME, "lib64"),
-          "-lcudart", "-Wl,-rpath,$ORIGIN"])
+          "-I", CSRC, src, png[0], "-o", CLI + ".tmp", "-L", HERE, "-lnli_dropin", "-lnli_gb300",
+          "-L", os.path.join(CUDA_HOME, "lib64"), "-lcudart", "-Wl,-rpath,$ORIGIN"])
     os.replace(CLI + ".tmp", CLI)
     return CLI
 

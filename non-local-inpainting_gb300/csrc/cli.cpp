@@ -10,12 +10,15 @@
 // -seed N (the reference seeds its generator with time(NULL)).  The image is
 // inpainted in CIE L*a*b* (:117, :307) with the conversions on the GPU.
 //
-// Image files: the reference reads and writes through libpng-backed iio;
-// here binary / ASCII PNM (P6, P5, P3, P2) and PFM (PF, Pf) are read, and
-// results are written as 8-bit P6 (rounded, clamped to 0..255) or, for a
-// name ending in ".pfm", as PFM.  The composed output name of :287-303 ends
-// in ".ppm" instead of ".png"; the inpainted depth goes to
-// inpainted_depth.pfm.
+// Image files: the reference reads and writes through iio on libpng; here
+// PNG (csrc/png_codec.cpp, the samples iio's reader returns), binary /
+// ASCII PNM (P6, P5, P3, P2) and PFM (PF, Pf) are read with iio's channel
+// rules (io_utility.cpp:120-170 over iio.c iio_read_image_float(_vec)), and
+// results are written as 8-bit PNG for names ending in ".png" (rounded and
+// clamped to 0..255 as iio converts floats), PFM for ".pfm" and binary
+// P6 / P5 otherwise.  The composed output name of :287-303 ends in ".png"
+// as the reference's.  The inpainted depth goes to inpainted_depth.pfm
+// (exact) and to inpainted_depth.png as 8-bit grey in all three channels.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,6 +32,7 @@
 #include <vector>
 
 #include "nli_inpainting.hpp"
+#include "png_codec.h"
 
 namespace {
 
@@ -51,10 +55,36 @@ const char *pick_option(int *c, char ***v, const char *name, const char *default
 }
 
 // ----------------------------------------------------------- image files
+// Samples as iio holds them: PNM and PFM are read into floats, PNG into
+// 8- or 16-bit integers; the kind matters for the grey conversion.
+enum SampleKind { kFloat, kU8, kU16 };
+
 struct Raster {
 	int W = 0, H = 0, C = 0;
+	SampleKind kind = kFloat;
 	std::vector<float> v;
 };
+
+Raster read_png(const std::string &name)
+{
+	FILE *f = fopen(name.c_str(), "rb");
+	if (!f) throw std::runtime_error("cannot open " + name);
+	std::vector<uint8_t> bytes;
+	unsigned char buf[65536];
+	size_t n;
+	while ((n = fread(buf, 1, sizeof(buf), f)) > 0) bytes.insert(bytes.end(), buf, buf + n);
+	fclose(f);
+	nli_png::Image im;
+	std::string err;
+	if (!nli_png::decode(bytes.data(), bytes.size(), im, err)) throw std::runtime_error(name + ": " + err);
+	Raster r;
+	r.W = im.width;
+	r.H = im.height;
+	r.C = im.channels;
+	r.kind = (im.depth == 16) ? kU16 : kU8;
+	r.v.assign(im.samples.begin(), im.samples.end());
+	return r;
+}
 
 int read_token(FILE *f)
 {
@@ -79,10 +109,17 @@ Raster read_image(const std::string &name)
 {
 	FILE *f = fopen(name.c_str(), "rb");
 	if (!f) throw std::runtime_error("cannot open " + name);
+	unsigned char sig[8] = {0};
+	const size_t got = fread(sig, 1, 8, f);
+	if (nli_png::is_png(sig, got)) {
+		fclose(f);
+		return read_png(name);
+	}
+	rewind(f);
 	char m[3] = {0, 0, 0};
 	if (fread(m, 1, 2, f) != 2 || m[0] != 'P') {
 		fclose(f);
-		throw std::runtime_error(name + ": not a PNM or PFM file (libpng formats are not supported)");
+		throw std::runtime_error(name + ": not a PNG, PNM or PFM file");
 	}
 	Raster r;
 	if (m[1] == 'F' || m[1] == 'f') {
@@ -146,36 +183,81 @@ Raster read_image(const std::string &name)
 	return r;
 }
 
-Image<float> to_image(const Raster &r, int C)
+// IOUtility::read_rgb_image (io_utility.cpp:150-171): channels 0, 1, 2,
+// the second and third taken from the first when the file has fewer (so a
+// grey + alpha file gives grey, alpha, grey).
+Image<float> rgb_image(const Raster &r)
 {
-	Image<float> im((uint)r.W, (uint)r.H, (uint)C);
+	Image<float> im((uint)r.W, (uint)r.H, 3u);
 	float *d = im.raw();
-	for (size_t p = 0; p < (size_t)r.W * r.H; p++)
-		for (int c = 0; c < C; c++) d[p * C + c] = r.v[p * r.C + std::min(c, r.C - 1)];
+	for (size_t p = 0; p < (size_t)r.W * r.H; p++) {
+		const float *s = &r.v[p * r.C];
+		d[3 * p] = s[0];
+		d[3 * p + 1] = r.C > 1 ? s[1] : s[0];
+		d[3 * p + 2] = r.C > 2 ? s[2] : s[0];
+	}
 	return im;
 }
 
+// IOUtility::read_mono_image (io_utility.cpp:120-145) over iio's
+// iio_read_image_float: one channel as it is; three or four channels to
+// 0.299 R + 0.587 G + 0.114 B in double (iio_hacky_uncolorize(a)), stored
+// back into the file's sample type (truncated for 8-bit PNG, a float for
+// PNM and PFM); 16-bit colour and grey + alpha files are refused.
+Image<float> mono_image(const Raster &r, const std::string &name)
+{
+	const bool colour = r.C == 3 || r.C == 4;
+	if (!(r.C == 1 || colour) || (colour && r.kind == kU16))
+		throw std::runtime_error("read_mono_image: cannot read " + name);
+	Image<float> im((uint)r.W, (uint)r.H, 1u);
+	float *d = im.raw();
+	for (size_t p = 0; p < (size_t)r.W * r.H; p++) {
+		const float *s = &r.v[p * r.C];
+		if (!colour) {
+			d[p] = s[0];
+		} else {
+			const double g = .299 * s[0] + .587 * s[1] + .114 * s[2];
+			d[p] = (r.kind == kU8) ? (float)(uint8_t)g : (float)g;
+		}
+	}
+	return im;
+}
+
+bool ends_with(const std::string &s, const char *suffix)
+{
+	const size_t n = strlen(suffix);
+	return s.size() >= n && s.compare(s.size() - n, n, suffix) == 0;
+}
+
+// iio's float to byte conversion: T8(0.5 + v), 0..255 (iio.c convert_datum)
+unsigned char to_byte(float v) { return (unsigned char)std::min(255.0f, std::max(0.0f, std::round(v))); }
+
 void write_image(const std::string &name, const float *v, int W, int H, int C)
 {
+	if (ends_with(name, ".png") || ends_with(name, ".PNG")) {
+		std::vector<uint8_t> b((size_t)W * H * C);
+		for (size_t i = 0; i < b.size(); i++) b[i] = to_byte(v[i]);
+		const std::vector<uint8_t> png = nli_png::encode8(b.data(), W, H, C);
+		FILE *f = fopen(name.c_str(), "wb");
+		if (!f) throw std::runtime_error("cannot write " + name);
+		const size_t put = fwrite(png.data(), 1, png.size(), f);
+		fclose(f);
+		if (put != png.size()) throw std::runtime_error("cannot write " + name);
+		return;
+	}
 	FILE *f = fopen(name.c_str(), "wb");
 	if (!f) throw std::runtime_error("cannot write " + name);
-	const bool pfm = name.size() > 4 && name.compare(name.size() - 4, 4, ".pfm") == 0;
+	const bool pfm = ends_with(name, ".pfm");
 	if (pfm) {
 		fprintf(f, "%s\n%d %d\n-1.0\n", C == 3 ? "PF" : "Pf", W, H);
 		for (int y = H - 1; y >= 0; y--) fwrite(v + (size_t)y * W * C, sizeof(float), (size_t)W * C, f);
 	} else {
 		fprintf(f, "%s\n%d %d\n255\n", C == 3 ? "P6" : "P5", W, H);
 		std::vector<unsigned char> b((size_t)W * H * C);
-		for (size_t i = 0; i < b.size(); i++) b[i] = (unsigned char)std::min(255.0f, std::max(0.0f, std::round(v[i])));
+		for (size_t i = 0; i < b.size(); i++) b[i] = to_byte(v[i]);
 		fwrite(b.data(), 1, b.size(), f);
 	}
 	fclose(f);
-}
-
-std::string with_ppm(std::string name)
-{
-	if (name.size() > 4 && name.compare(name.size() - 4, 4, ".png") == 0) name.replace(name.size() - 4, 4, ".ppm");
-	return name;
 }
 
 // ------------------------------------------------ GPU helpers (C ABI)
@@ -267,16 +349,16 @@ int run(int argc, char *argv[])
 	}
 	const std::string input_name = argv[1], mask_name = argv[2], output_name = argv[3];
 
-	Image<float> input = convert(to_image(read_image(input_name), 3), true);
-	Raster mask_raster = read_image(mask_name);
-	if (input.get_size_x() != (uint)mask_raster.W || input.get_size_y() != (uint)mask_raster.H)
+	Image<float> input = convert(rgb_image(read_image(input_name)), true);
+	Image<float> mask_image = mono_image(read_image(mask_name), mask_name);
+	if (input.get_size_x() != mask_image.get_size_x() || input.get_size_y() != mask_image.get_size_y())
 		throw std::runtime_error("ERROR: Input image and mask should be of the same size");
 	bool is_mask_empty = true;
-	Mask mask((uint)mask_raster.W, (uint)mask_raster.H);
-	for (int y = 0; y < mask_raster.H; y++)
-		for (int x = 0; x < mask_raster.W; x++)
-			if (mask_raster.v[((size_t)y * mask_raster.W + x) * mask_raster.C] > 0) {
-				mask.mask((uint)x, (uint)y);
+	Mask mask(mask_image.get_size_x(), mask_image.get_size_y());
+	for (uint y = 0; y < mask_image.get_size_y(); y++)
+		for (uint x = 0; x < mask_image.get_size_x(); x++)
+			if (mask_image.raw()[(size_t)y * mask_image.get_size_x() + x] > 0) {
+				mask.mask(x, y);
 				is_mask_empty = false;
 			}
 	if (is_mask_empty) throw std::runtime_error("ERROR: Mask should not be empty (all black)");
@@ -284,7 +366,7 @@ int run(int argc, char *argv[])
 	bool depth_exists = false;
 	if (!depth_name.empty()) {
 		depth_exists = true;
-		Image<float> depth = to_image(read_image(depth_name), 1);
+		Image<float> depth = mono_image(read_image(depth_name), depth_name);
 		if (depth.get_size_x() != input.get_size_x() || depth.get_size_y() != input.get_size_y())
 			throw std::runtime_error("cat: Size does not match.");
 		Image<float> rgbd(input.get_size_x(), input.get_size_y(), 4u);
@@ -372,18 +454,19 @@ int run(int argc, char *argv[])
 	output_str << "_conf" << confidence_decay_time << "_" << confidence_asymptotic_value << ".png";
 	const int W = output.get_size_x(), H = output.get_size_y(), C = output.get_number_of_channels();
 	Image<float> rgb = convert(output, false);
-	write_image(with_ppm(output_str.str()), rgb.raw(), W, H, 3);
-	printf("%s\n", with_ppm(output_str.str()).c_str());
+	write_image(output_str.str(), rgb.raw(), W, H, 3);
+	printf("%s\n", output_str.str().c_str());
 	if (depth_exists) {
-		std::vector<float> d((size_t)W * H);
-		for (size_t p = 0; p < d.size(); p++) d[p] = output.raw()[(size_t)C * p + 3];
+		std::vector<float> d((size_t)W * H), d3((size_t)W * H * 3);
+		for (size_t p = 0; p < d.size(); p++) d[p] = d3[3 * p] = d3[3 * p + 1] = d3[3 * p + 2] = output.raw()[(size_t)C * p + 3];
 		write_image("inpainted_depth.pfm", d.data(), W, H, 1);
+		write_image("inpainted_depth.png", d3.data(), W, H, 3);
 	}
 	if (!show_pyramid_file.empty()) {
 		std::vector<Image<float> > pyr = image_inpainting.get_output_image_pyramid();
 		for (size_t n = 0; n < pyr.size(); n++) {
 			std::stringstream s;
-			s << show_pyramid_file << n << ".ppm";
+			s << show_pyramid_file << n << ".png";
 			Image<float> lv = convert(pyr[n], false);
 			write_image(s.str(), lv.raw(), lv.get_size_x(), lv.get_size_y(), 3);
 		}
@@ -407,7 +490,7 @@ int run(int argc, char *argv[])
 						if (u.x - x != b.x - x || u.y - (y - 1) != b.y - y) sv[((size_t)y * W + x) * 3 + c] = 0;
 					}
 				}
-		write_image(with_ppm(show_nnf_file), sv, W, H, 3);
+		write_image(show_nnf_file, sv, W, H, 3);
 	}
 	return 0;
 }

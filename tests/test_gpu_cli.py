@@ -3,7 +3,9 @@ against the reference's (golden vectors), RGB-D packing, and nli_inpaint
 (main.cpp's program on the drop-in classes) against the same steps driven
 through the C ABI."""
 import os
+import struct
 import subprocess
+import zlib
 
 import numpy as np
 import pytest
@@ -47,13 +49,40 @@ def write_pnm(path, a):
         f.write(a.tobytes())
 
 
-def read_pnm(path):
-    with open(path, "rb") as f:
-        data = f.read()
-    parts = data.split(b"\n", 3)
-    W, H = map(int, parts[1].split())
-    C = 3 if parts[0] == b"P6" else 1
-    return np.frombuffer(parts[3], np.uint8).reshape(H, W, C)
+def write_png(path, a):
+    """8-bit PNG of an (H, W) or (H, W, C) array with the standard library."""
+    a = np.asarray(a, np.uint8)
+    if a.ndim == 2:
+        a = a[..., None]
+    H, W, C = a.shape
+    raw = b"".join(b"\x00" + a[y].tobytes() for y in range(H))
+
+    def chunk(kind, body):
+        return struct.pack(">I", len(body)) + kind + body + struct.pack(">I", zlib.crc32(kind + body) & 0xffffffff)
+    color = {1: 0, 2: 4, 3: 2, 4: 6}[C]
+    data = (b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", W, H, 8, color, 0, 0, 0)) +
+            chunk(b"IDAT", zlib.compress(raw, 6)) + chunk(b"IEND", b""))
+    with open(path, "wb") as f:
+        f.write(data)
+
+
+def read_png(path):
+    """The program's PNG output: 8-bit, rows with filter type 0."""
+    data = open(path, "rb").read()
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+    pos, idat = 8, b""
+    while pos < len(data):
+        n = struct.unpack(">I", data[pos:pos + 4])[0]
+        kind, body = data[pos + 4:pos + 8], data[pos + 8:pos + 8 + n]
+        if kind == b"IHDR":
+            W, H, depth, color = struct.unpack(">IIBB", body[:10])
+        elif kind == b"IDAT":
+            idat += body
+        pos += 12 + n
+    C = {0: 1, 4: 2, 2: 3, 6: 4}[color]
+    rows = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(H, W * C + 1)
+    assert depth == 8 and (rows[:, 0] == 0).all()
+    return rows[:, 1:].reshape(H, W, C)
 
 
 @pytest.fixture(scope="module")
@@ -70,13 +99,13 @@ def test_cli_matches_c_abi(cli, gpu_ctx, tmp_path):
     write_pnm(tmp_path / "in.ppm", img8)
     write_pnm(tmp_path / "mask.pgm", mask * 255)
     r = subprocess.run([cli, "in.ppm", "mask.pgm", "out", "-method", "nlmeans", "-patch", "9", "-scales", "3",
-                        "-coarse", "0.5", "-iters", "10", "-seed", "5", "-shownnf", "nnf.ppm", "-showpyr", "pyr_"],
+                        "-coarse", "0.5", "-iters", "10", "-seed", "5", "-shownnf", "nnf.png", "-showpyr", "pyr_"],
                        cwd=tmp_path, capture_output=True, text=True)
     print(r.stdout, r.stderr)
     assert r.returncode == 0, r.stderr
-    name = "out_nlmeans_sc3_0.5_initnone_ps9_10000_conf5_0.1.ppm"  # main.cpp's composed name
+    name = "out_nlmeans_sc3_0.5_initnone_ps9_10000_conf5_0.1.png"  # main.cpp's composed name
     assert name in r.stdout
-    got = read_pnm(tmp_path / name)
+    got = read_png(tmp_path / name)
     # the same steps through the C ABI: Lab, process with the CLI's pairing
     # (nlmeans with L2Norm distances), back to RGB, rounded
     p = wl.params("nlmeans", distance="l2", patch=9, scales=3, coarse=0.5, iters=10)
@@ -91,9 +120,40 @@ def test_cli_matches_c_abi(cli, gpu_ctx, tmp_path):
     known = mask == 0
     assert np.abs(got[known].astype(int) - img8[known].astype(int)).max() <= 1  # Lab round trip
     for n in range(3):
-        assert (tmp_path / ("pyr_%d.ppm" % n)).exists()
-    nnf_img = read_pnm(tmp_path / "nnf.ppm")
+        assert read_png(tmp_path / ("pyr_%d.png" % n)).shape[2] == 3
+    nnf_img = read_png(tmp_path / "nnf.png")
     assert nnf_img.shape == got.shape and (nnf_img == 0).any()
+
+
+def test_cli_png_inputs_and_channel_rules(cli, gpu_ctx, tmp_path):
+    """PNG input and mask files, read with iio's rules: a grey + alpha image
+    gives (grey, alpha, grey); a colour mask is reduced to
+    0.299 R + 0.587 G + 0.114 B truncated to a byte, so (1, 0, 0) is not a
+    hole pixel and (0, 2, 0) is."""
+    from nli_gb300 import workloads as wl
+    img, mask, _ = wl.config2(seed=9, size=64, scales=3)
+    grey = np.clip(np.round(img[..., 0]), 0, 255).astype(np.uint8)
+    alpha = np.clip(np.round(img[..., 1]), 0, 255).astype(np.uint8)
+    write_png(tmp_path / "in.png", np.stack([grey, alpha], -1))
+    cmask = np.zeros(mask.shape + (3,), np.uint8)
+    cmask[mask != 0] = (0, 2, 0)
+    decoy = (mask == 0) & (np.arange(mask.size).reshape(mask.shape) % 7 == 0)
+    cmask[decoy] = (1, 0, 0)
+    write_png(tmp_path / "mask.png", cmask)
+    r = subprocess.run([cli, "in.png", "mask.png", "out", "-method", "nlmeans", "-patch", "9", "-scales", "3",
+                        "-coarse", "0.5", "-iters", "8", "-seed", "3"], cwd=tmp_path, capture_output=True, text=True)
+    print(r.stdout, r.stderr)
+    assert r.returncode == 0, r.stderr
+    got = read_png(tmp_path / "out_nlmeans_sc3_0.5_initnone_ps9_10000_conf5_0.1.png")
+    rgb = np.stack([grey, alpha, grey], -1).astype(np.float32)
+    p = wl.params("nlmeans", distance="l2", patch=9, scales=3, coarse=0.5, iters=8)
+    p.patchmatch.random_shots = 30
+    lab = gpu_ctx.rgb_to_lab(rgb).cpu().numpy()
+    gpu_ctx.set_seed(3)
+    out, _ = gpu_ctx.process(lab, (mask != 0).astype(np.uint8), p)
+    v = gpu_ctx.lab_to_rgb(out).cpu().numpy().astype(np.float64)
+    v = np.where(v >= 0, np.floor(v + 0.5), np.ceil(v - 0.5))
+    assert np.array_equal(got, np.clip(v, 0, 255).astype(np.uint8))
 
 
 def test_cli_errors(cli, tmp_path):
@@ -129,3 +189,6 @@ def test_cli_depth(cli, tmp_path):
     known = mask == 0
     assert np.array_equal(out_d[known], d[known])  # known depth untouched
     assert np.isfinite(out_d).all() and (out_d[~known] > 0.3).all()
+    dpng = read_png(tmp_path / "inpainted_depth.png")
+    want = np.clip(np.floor(out_d.astype(np.float64) + 0.5), 0, 255).astype(np.uint8)
+    assert np.array_equal(dpng, np.repeat(want[..., None], 3, -1))
