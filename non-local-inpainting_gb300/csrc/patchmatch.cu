@@ -36,6 +36,8 @@
 // strict "<", so the result equals evaluating them one after the other.
 #include <cuda.h>  // CUtensorMap (the descriptor type; encoded through the runtime's driver entry point)
 
+#include <atomic>
+
 #include "nli_device.cuh"
 
 namespace nli {
@@ -828,8 +830,21 @@ static void launch_sweeps(nli_ctx *ctx, const DistArgs &a, const PmArgs &p, int 
 	const int block = pm_threads(V);
 	const int grid = (int)std::min<size_t>(((size_t)p.nt * 32 + block - 1) / block, (size_t)ctx->num_sms);
 	int *timeout = &ctx->status->timeout;
-	NLI_CUDA(cudaFuncSetAttribute(k_pm_init<KIND, C, P, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-	NLI_CUDA(cudaFuncSetAttribute(k_pm_sweep<KIND, C, P, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+	// The kernels' dynamic shared-memory limit is raised once per device, to
+	// the largest opt-in size (each launch passes the size it uses): a
+	// function attribute set on every call costs a driver call per PatchMatch
+	// call on every batch worker thread.
+	static std::atomic<uint32_t> raised{0};  // one bit per device
+	const uint32_t bit = 1u << (ctx->device & 31);
+	if (!(raised.load(std::memory_order_acquire) & bit)) {
+		NLI_REQUIRE(smem <= (size_t)ctx->max_smem_optin, NLI_E_UNSUPPORTED, "PatchMatch shared memory too large");
+		NLI_CUDA(cudaFuncSetAttribute(k_pm_init<KIND, C, P, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                              ctx->max_smem_optin));
+		NLI_CUDA(cudaFuncSetAttribute(k_pm_sweep<KIND, C, P, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                              ctx->max_smem_optin));
+		raised.fetch_or(bit, std::memory_order_release);
+	}
+	NLI_REQUIRE(smem <= (size_t)ctx->max_smem_optin, NLI_E_UNSUPPORTED, "PatchMatch shared memory too large");
 	{
 		ProfScope ps(ctx, "pm_init");
 		k_pm_init<KIND, C, P, V><<<grid, block, smem, ctx->stream>>>(a, p, init, nnf_x, dist_x, counter, map,
