@@ -568,6 +568,113 @@ bool decode(const uint8_t *data, size_t size, Image &out, std::string &error)
 	return true;
 }
 
+namespace {
+
+// LSB-first bit packing of a DEFLATE stream
+struct BitWriter {
+	std::vector<uint8_t> &out;
+	uint32_t buf = 0;
+	int count = 0;
+	explicit BitWriter(std::vector<uint8_t> &o) : out(o) {}
+	void put(uint32_t v, int n)
+	{
+		buf |= v << count;
+		count += n;
+		while (count >= 8) {
+			out.push_back((uint8_t)buf);
+			buf >>= 8;
+			count -= 8;
+		}
+	}
+	// a Huffman code: its bits go out most significant first
+	void code(uint32_t c, int n)
+	{
+		uint32_t r = 0;
+		for (int k = 0; k < n; k++) r |= ((c >> k) & 1u) << (n - 1 - k);
+		put(r, n);
+	}
+	void flush()
+	{
+		if (count > 0) out.push_back((uint8_t)buf);
+		buf = 0;
+		count = 0;
+	}
+};
+
+// literal / length symbol in the fixed code of RFC 1951 section 3.2.6
+void fixed_symbol(BitWriter &w, int s)
+{
+	if (s < 144)
+		w.code(0x30 + s, 8);
+	else if (s < 256)
+		w.code(0x190 + (s - 144), 9);
+	else if (s < 280)
+		w.code(s - 256, 7);
+	else
+		w.code(0xC0 + (s - 280), 8);
+}
+
+// One fixed-Huffman DEFLATE block over the whole input, with greedy LZ77
+// matches found through 3-byte hash chains (window 32 KiB, matches 3..258).
+std::vector<uint8_t> deflate_fixed(const uint8_t *in, size_t n)
+{
+	std::vector<uint8_t> out;
+	BitWriter w(out);
+	w.put(1, 1);  // last block
+	w.put(1, 2);  // fixed codes
+	constexpr int kHashBits = 15, kChain = 48;
+	constexpr size_t kWindow = 32768, kMaxMatch = 258;
+	std::vector<int32_t> head((size_t)1 << kHashBits, -1), prev(n, -1);
+	auto hash = [&](size_t i) {
+		const uint32_t v = (uint32_t)in[i] << 16 | (uint32_t)in[i + 1] << 8 | in[i + 2];
+		return (v * 2654435761u) >> (32 - kHashBits);
+	};
+	auto insert = [&](size_t i) {
+		if (i + 2 >= n) return;
+		const uint32_t h = hash(i);
+		prev[i] = head[h];
+		head[h] = (int32_t)i;
+	};
+	size_t i = 0;
+	while (i < n) {
+		size_t best = 0, best_dist = 0;
+		if (i + 2 < n) {
+			const size_t limit = std::min(kMaxMatch, n - i);
+			int32_t cand = head[hash(i)];
+			for (int k = 0; k < kChain && cand >= 0 && i - (size_t)cand <= kWindow; k++, cand = prev[cand]) {
+				size_t len = 0;
+				while (len < limit && in[cand + len] == in[i + len]) len++;
+				if (len > best) {
+					best = len;
+					best_dist = i - (size_t)cand;
+					if (len == limit) break;
+				}
+			}
+		}
+		if (best >= 3) {
+			int li = 28;
+			while (kLenBase[li] > best) li--;
+			fixed_symbol(w, 257 + li);
+			w.put((uint32_t)(best - kLenBase[li]), kLenExtra[li]);
+			int di = 29;
+			while (kDistBase[di] > best_dist) di--;
+			w.code((uint32_t)di, 5);
+			w.put((uint32_t)(best_dist - kDistBase[di]), kDistExtra[di]);
+			for (size_t k = 0; k < best; k++) insert(i + k);
+			i += best;
+		} else {
+			fixed_symbol(w, in[i]);
+			insert(i);
+			i++;
+		}
+	}
+	fixed_symbol(w, 256);
+	w.flush();
+	return out;
+}
+
+}  // namespace
+
 std::vector<uint8_t> encode8(const uint8_t *samples, int width, int height, int channels)
 {
 	static const uint8_t colour[5] = {0, 0, 4, 2, 6};
@@ -585,31 +692,44 @@ std::vector<uint8_t> encode8(const uint8_t *samples, int width, int height, int 
 	ihdr.push_back(8);
 	ihdr.push_back(colour[channels]);
 	ihdr.push_back(0);  // deflate
-	ihdr.push_back(0);  // adaptive filtering (each row: type 0)
+	ihdr.push_back(0);  // adaptive filtering
 	ihdr.push_back(0);  // not interlaced
 	chunk("IHDR", ihdr);
-	// the filtered image: each row preceded by filter type 0
+	// each row with the filter of smallest sum of |signed residual| (the
+	// usual adaptive heuristic)
 	const size_t rb = (size_t)width * channels;
+	const int bpp = channels;
 	std::vector<uint8_t> filtered;
 	filtered.reserve((size_t)height * (rb + 1));
+	std::vector<uint8_t> trial[5];
+	for (auto &t : trial) t.resize(rb);
 	for (int y = 0; y < height; y++) {
-		filtered.push_back(0);
-		filtered.insert(filtered.end(), samples + (size_t)y * rb, samples + (size_t)(y + 1) * rb);
+		const uint8_t *r = samples + (size_t)y * rb;
+		const uint8_t *up = y > 0 ? r - rb : nullptr;
+		uint64_t best_cost = UINT64_MAX;
+		int best = 0;
+		for (int f = 0; f < 5; f++) {
+			uint64_t cost = 0;
+			for (size_t i = 0; i < rb; i++) {
+				const int a = (i >= (size_t)bpp) ? r[i - bpp] : 0;
+				const int b = up ? up[i] : 0;
+				const int c = (up && i >= (size_t)bpp) ? up[i - bpp] : 0;
+				const int pred = f == 0 ? 0 : f == 1 ? a : f == 2 ? b : f == 3 ? ((a + b) >> 1) : paeth(a, b, c);
+				const uint8_t v = (uint8_t)(r[i] - pred);
+				trial[f][i] = v;
+				cost += (uint64_t)(v < 128 ? v : 256 - v);
+			}
+			if (cost < best_cost) {
+				best_cost = cost;
+				best = f;
+			}
+		}
+		filtered.push_back((uint8_t)best);
+		filtered.insert(filtered.end(), trial[best].begin(), trial[best].end());
 	}
-	// zlib stream of stored DEFLATE blocks
 	std::vector<uint8_t> z = {0x78, 0x01};
-	size_t off = 0;
-	do {
-		const size_t n = std::min<size_t>(65535, filtered.size() - off);
-		const bool last = off + n == filtered.size();
-		z.push_back(last ? 1 : 0);
-		z.push_back((uint8_t)n);
-		z.push_back((uint8_t)(n >> 8));
-		z.push_back((uint8_t)~n);
-		z.push_back((uint8_t)(~n >> 8));
-		z.insert(z.end(), filtered.begin() + off, filtered.begin() + off + n);
-		off += n;
-	} while (off < filtered.size());
+	const std::vector<uint8_t> d = deflate_fixed(filtered.data(), filtered.size());
+	z.insert(z.end(), d.begin(), d.end());
 	put32(z, adler32(filtered.data(), filtered.size()));
 	chunk("IDAT", z);
 	chunk("IEND", {});

@@ -10,8 +10,9 @@
 // to 8 bits, a tRNS colour key becomes an alpha channel, and 16-bit samples
 // stay 16-bit.  Interlaced (Adam7) images are supported.
 //
-// Encoding writes 8-bit grey, grey + alpha, RGB or RGBA images with
-// unfiltered rows in stored (uncompressed) DEFLATE blocks.
+// Encoding writes 8-bit grey, grey + alpha, RGB or RGBA images, each row
+// with the adaptive filter of smallest residual, compressed with the fixed
+// Huffman code of DEFLATE over greedy LZ77 matches.
 #pragma once
 
 #include <cstddef>

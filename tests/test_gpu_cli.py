@@ -66,8 +66,14 @@ def write_png(path, a):
         f.write(data)
 
 
+def paeth(a, b, c):
+    p = a + b - c
+    pa, pb, pc = abs(p - a), abs(p - b), abs(p - c)
+    return a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
+
+
 def read_png(path):
-    """The program's PNG output: 8-bit, rows with filter type 0."""
+    """The program's PNG output: 8-bit, adaptive row filters."""
     data = open(path, "rb").read()
     assert data[:8] == b"\x89PNG\r\n\x1a\n"
     pos, idat = 8, b""
@@ -80,9 +86,17 @@ def read_png(path):
             idat += body
         pos += 12 + n
     C = {0: 1, 4: 2, 2: 3, 6: 4}[color]
+    assert depth == 8
     rows = np.frombuffer(zlib.decompress(idat), np.uint8).reshape(H, W * C + 1)
-    assert depth == 8 and (rows[:, 0] == 0).all()
-    return rows[:, 1:].reshape(H, W, C)
+    out = np.zeros((H, W * C), np.int64)
+    for y in range(H):
+        t, r = int(rows[y, 0]), rows[y, 1:].astype(np.int64)
+        up = out[y - 1] if y > 0 else np.zeros(W * C, np.int64)
+        for i in range(W * C):
+            a = out[y, i - C] if i >= C else 0
+            c = up[i - C] if i >= C else 0
+            out[y, i] = (r[i] + [0, a, up[i], (a + up[i]) >> 1, paeth(a, up[i], c)][t]) & 0xff
+    return out.astype(np.uint8).reshape(H, W, C)
 
 
 @pytest.fixture(scope="module")

@@ -214,8 +214,27 @@ def test_rejects_corrupt_files(tool, tmp_path):
         assert got is None and err, name
 
 
+def unfilter8(raw, H, W, C):
+    """Reverses the row filters of an 8-bit image (bytes per pixel C)."""
+    stride = W * C
+    rows = np.frombuffer(raw, np.uint8).reshape(H, stride + 1)
+    out = np.zeros((H, stride), np.int64)
+    for y in range(H):
+        t, r = rows[y, 0], rows[y, 1:].astype(np.int64)
+        up = out[y - 1] if y > 0 else np.zeros(stride, np.int64)
+        cur = np.zeros(stride, np.int64)
+        for i in range(stride):
+            a = cur[i - C] if i >= C else 0
+            b = up[i]
+            c = up[i - C] if i >= C else 0
+            pred = [0, a, b, (a + b) >> 1, paeth(a, b, c)][t]
+            cur[i] = (r[i] + pred) & 0xff
+        out[y] = cur
+    return out.astype(np.uint8).reshape(H, W, C)
+
+
 def read_png_python(data):
-    """Minimal reader for the encoder's output (8-bit, filter 0 rows)."""
+    """Reader for the encoder's output (8-bit, any row filters)."""
     assert data[:8] == b"\x89PNG\r\n\x1a\n"
     pos, idat, hdr = 8, b"", None
     while pos < len(data):
@@ -229,17 +248,20 @@ def read_png_python(data):
         pos += 12 + n
     W, H, depth, color = hdr[:4]
     C = {0: 1, 4: 2, 2: 3, 6: 4}[color]
-    raw = zlib.decompress(idat)
-    rows = np.frombuffer(raw, np.uint8).reshape(H, W * C + 1)
-    assert (rows[:, 0] == 0).all() and depth == 8
-    return rows[:, 1:].reshape(H, W, C)
+    assert depth == 8
+    return unfilter8(zlib.decompress(idat), H, W, C)
 
 
 @pytest.mark.parametrize("C", [1, 2, 3, 4])
 def test_encoder(tool, tmp_path, C):
+    """Random (incompressible) and smooth images: zlib inflates the stream,
+    the filters undo to the input, and the smooth image compresses."""
     rng = np.random.default_rng(C)
-    for (W, H) in ((1, 1), (37, 23), (400, 200)):  # 400x200x4 spans several stored blocks
-        img = rng.integers(0, 256, (H, W, C)).astype(np.uint8)
+    y, x = np.mgrid[0:120, 0:160]
+    smooth = np.stack([(x + y) % 256, (2 * x) % 256, (y * 3) % 256, np.full_like(x, 200)], -1)[..., :C]
+    for img in (rng.integers(0, 256, (1, 1, C)), rng.integers(0, 256, (23, 37, C)), smooth):
+        img = np.ascontiguousarray(img).astype(np.uint8)
+        H, W = img.shape[:2]
         src, dst = str(tmp_path / "raw"), str(tmp_path / "o.png")
         img.tofile(src)
         subprocess.run([tool, "encode", str(W), str(H), str(C), src, dst], check=True)
@@ -247,3 +269,5 @@ def test_encoder(tool, tmp_path, C):
         assert np.array_equal(read_png_python(data), img)
         (samples, d), err = decode(tool, tmp_path, data)  # and our own decoder reads it back
         assert np.array_equal(samples, img)
+        if img is smooth or H == 120:
+            assert len(data) < img.size // 4, (len(data), img.size)
