@@ -11,20 +11,25 @@
 namespace nli_png {
 
 // ------------------------------------------------------------ checksums
-uint32_t crc32(const uint8_t *data, size_t size, uint32_t crc)
-{
-	static uint32_t table[256];
-	static bool ready = false;
-	if (!ready) {
+namespace {
+struct CrcTable {
+	uint32_t v[256];
+	CrcTable()
+	{
 		for (uint32_t n = 0; n < 256; n++) {
 			uint32_t c = n;
 			for (int k = 0; k < 8; k++) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : (c >> 1);
-			table[n] = c;
+			v[n] = c;
 		}
-		ready = true;
 	}
+};
+}  // namespace
+
+uint32_t crc32(const uint8_t *data, size_t size, uint32_t crc)
+{
+	static const CrcTable table;  // initialised once, thread-safe
 	crc = ~crc;
-	for (size_t i = 0; i < size; i++) crc = table[(crc ^ data[i]) & 0xff] ^ (crc >> 8);
+	for (size_t i = 0; i < size; i++) crc = table.v[(crc ^ data[i]) & 0xff] ^ (crc >> 8);
 	return ~crc;
 }
 
@@ -203,21 +208,23 @@ bool inflate_raw(Bits &in, std::vector<uint8_t> &out, size_t limit, std::string 
 			out.insert(out.end(), in.p + in.pos, in.p + in.pos + len);
 			in.pos += len;
 		} else if (type == 1) {  // fixed Huffman codes
-			static Huffman lit, dist;
-			static bool ready = false;
-			if (!ready) {
-				uint8_t l[288];
-				for (int s = 0; s < 144; s++) l[s] = 8;
-				for (int s = 144; s < 256; s++) l[s] = 9;
-				for (int s = 256; s < 280; s++) l[s] = 7;
-				for (int s = 280; s < 288; s++) l[s] = 8;
-				build(lit, l, 288);
-				uint8_t dl[30];
-				for (int s = 0; s < 30; s++) dl[s] = 5;
-				build(dist, dl, 30);
-				ready = true;
-			}
-			if (!codes(in, out, lit, dist, limit, error)) return false;
+			struct Fixed {
+				Huffman lit, dist;
+				Fixed()
+				{
+					uint8_t l[288];
+					for (int s = 0; s < 144; s++) l[s] = 8;
+					for (int s = 144; s < 256; s++) l[s] = 9;
+					for (int s = 256; s < 280; s++) l[s] = 7;
+					for (int s = 280; s < 288; s++) l[s] = 8;
+					build(lit, l, 288);
+					uint8_t dl[30];
+					for (int s = 0; s < 30; s++) dl[s] = 5;
+					build(dist, dl, 30);
+				}
+			};
+			static const Fixed fixed;  // initialised once, thread-safe
+			if (!codes(in, out, fixed.lit, fixed.dist, limit, error)) return false;
 		} else if (type == 2) {  // dynamic Huffman codes
 			const int nlen = (int)in.take(5) + 257, ndist = (int)in.take(5) + 1, ncode = (int)in.take(4) + 4;
 			if (nlen > 286 || ndist > 30) {
