@@ -484,9 +484,11 @@ bool decode(const uint8_t *data, size_t size, Image &out, std::string &error)
 	const int bpp = std::max(1, rc * d / 8);
 	// defiltered raw pixels of the whole image, rows of rowbytes(W) bytes
 	auto rowbytes = [&](int w) { return ((size_t)w * rc * d + 7) / 8; };
+	// the inflated size is bounded (extra data after the image, which libpng
+	// tolerates, is accepted up to 1 MiB and ignored)
 	const size_t expected = h.interlace ? (size_t)H * (rowbytes(W) + 1) * 2 + 64 : (size_t)H * (rowbytes(W) + 1);
 	std::vector<uint8_t> raw;
-	if (!inflate_zlib(idat.data(), idat.size(), raw, expected, error)) return false;
+	if (!inflate_zlib(idat.data(), idat.size(), raw, expected + (1u << 20), error)) return false;
 	std::vector<uint8_t> full((size_t)H * rowbytes(W));
 	static const int ax0[7] = {0, 4, 0, 2, 0, 1, 0}, ay0[7] = {0, 0, 4, 0, 2, 0, 1};
 	static const int adx[7] = {8, 8, 4, 4, 2, 2, 1}, ady[7] = {8, 8, 8, 4, 4, 2, 2};

@@ -271,3 +271,69 @@ def test_encoder(tool, tmp_path, C):
         assert np.array_equal(samples, img)
         if img is smooth or H == 120:
             assert len(data) < img.size // 4, (len(data), img.size)
+
+
+@pytest.fixture(scope="module")
+def checked_tool(tmp_path_factory):
+    """The test driver built with AddressSanitizer and UBSan (skipped where
+    the compiler lacks them)."""
+    out = str(tmp_path_factory.mktemp("png_asan") / "png_tool")
+    r = subprocess.run(["g++", "-O1", "-g", "-fsanitize=address,undefined", "-fno-sanitize-recover=undefined",
+                        "-std=c++17", "-I", CSRC, os.path.join(ROOT, "tests", "cpp", "png_tool.cpp"),
+                        os.path.join(CSRC, "png_codec.cpp"), "-o", out], capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip("no sanitizer runtime: " + r.stderr[-200:])
+    good = str(tmp_path_factory.mktemp("png_asan_probe") / "g.png")
+    with open(good, "wb") as f:
+        f.write(make_png(np.zeros((2, 2, 3), np.uint32), 2, 8))
+    r = subprocess.run([out, "decode", good, good + ".bin"], capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip("sanitized binaries do not run here: " + r.stderr[-200:])
+    return out
+
+
+def test_decoder_survives_corruption(checked_tool, tmp_path):
+    """Structure-aware corruption (chunk CRCs recomputed, so the inflater,
+    the filters and the expansion see the damage): every file is either
+    decoded or rejected with a message, with no sanitizer report."""
+    import random
+    rng, rnd = np.random.default_rng(11), random.Random(11)
+    seeds = []
+    for color, depth in CASES:
+        npal = min(1 << depth, 200) if color == 3 else None
+        raw = random_raw(rng, color, depth, 9, 7, npal)
+        pal = rng.integers(0, 256, (npal, 3)) if color == 3 else None
+        png = make_png(raw, color, depth, pal, None, interlace=bool(rng.integers(2)), filters=(0, 1, 2, 3, 4),
+                       level=int(rng.integers(0, 10)))
+        pos, chunks = 8, []
+        while pos < len(png):
+            n = struct.unpack(">I", png[pos:pos + 4])[0]
+            chunks.append((png[pos + 4:pos + 8], png[pos + 8:pos + 8 + n]))
+            pos += 12 + n
+        seeds.append(chunks)
+    outcomes = {0: 0, 2: 0}
+    for it in range(300):
+        chunks = []
+        mode = rnd.random()
+        for kind, body in rnd.choice(seeds):
+            b = bytearray(body)
+            if kind == b"IDAT" and mode < 0.4 and b:
+                for _ in range(rnd.randint(1, 4)):
+                    b[rnd.randrange(len(b))] = rnd.randrange(256)
+            elif kind == b"IDAT" and mode < 0.8:
+                data = bytearray(zlib.decompress(bytes(b)))
+                for _ in range(rnd.randint(1, 4)):
+                    data[rnd.randrange(len(data))] = rnd.randrange(256)
+                data = data[:rnd.randrange(len(data) + 1)] if rnd.random() < 0.3 else data + bytes(rnd.randrange(40))
+                b = bytearray(zlib.compress(bytes(data), rnd.randrange(10)))
+            elif kind in (b"IHDR", b"PLTE") and mode >= 0.8 and b:
+                b[rnd.randrange(len(b))] = rnd.randrange(256)
+            chunks.append(chunk(kind, bytes(b)))
+        src = str(tmp_path / "f.png")
+        with open(src, "wb") as f:
+            f.write(b"\x89PNG\r\n\x1a\n" + b"".join(chunks))
+        r = subprocess.run([checked_tool, "decode", src, str(tmp_path / "f.bin")], capture_output=True, text=True)
+        assert r.returncode in (0, 2), (it, r.returncode, r.stderr[-800:])
+        assert r.returncode == 0 or r.stderr.strip()
+        outcomes[r.returncode] += 1
+    assert outcomes[0] > 10 and outcomes[2] > 10, outcomes
