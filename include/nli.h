@@ -244,8 +244,10 @@ int nli_distance_pairs(nli_ctx *ctx, const nli_distance_params *dist,
  * device array of NLI_NOALLOC_SCRATCH_BYTES that every process loading this
  * library holds on each device it uses until exit.  Work is enqueued on
  * `stream` (a cudaStream_t, NULL = legacy default stream) of the current
- * device.  The first call on a device looks up the array's device address;
- * make that first call before any stream capture.  Returns NLI_E_INVALID
+ * device.  The first call in a CUDA context (a device's primary context, or
+ * a context the caller made current) looks up the array's device address in
+ * that context; make that first call before any stream capture.  A context
+ * re-created by cudaDeviceReset counts as a new one.  Returns NLI_E_INVALID
  * when the gradients needed (sW*sH*2C floats, plus tW*tH*2C when target is
  * a different image; none for the L2Norm/L1Norm kinds) exceed
  * NLI_NOALLOC_SCRATCH_BYTES.  All calls share the array: calls that overlap

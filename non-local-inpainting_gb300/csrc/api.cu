@@ -102,6 +102,9 @@ static int fail(nli_ctx *ctx, const Error &e)
 	catch (const std::bad_alloc &) {                                     \
 		return fail(ctx, Error{NLI_E_NOMEM, "host allocation failed"}); \
 	}                                                                    \
+	catch (const std::exception &e) {                                    \
+		return fail(ctx, Error{NLI_E_INVALID, e.what()});               \
+	}                                                                    \
 	return NLI_OK;
 
 static void require_ptrs(std::initializer_list<const void *> ps)

@@ -1,7 +1,11 @@
 // APatchDistance::calculate over explicit pair lists, and the exhaustive
 // nearest-neighbour search used to pin PatchMatch on small crops.  Both use
 // the reference-exact distance (nli_device.cuh, dist_exact).
+#include <cuda.h>  // CUcontext, CUresult (driver entry points reached through the runtime)
+
 #include <mutex>
+#include <new>
+#include <stdexcept>
 
 #include "nli_device.cuh"
 
@@ -114,6 +118,12 @@ extern "C" int nli_distance_pairs(nli_ctx *ctx, const nli_distance_params *dist,
 	} catch (const Error &e) {
 		ctx->last_error = e.message;
 		return e.status;
+	} catch (const std::bad_alloc &) {
+		ctx->last_error = "host allocation failed";
+		return NLI_E_NOMEM;
+	} catch (const std::exception &e) {
+		ctx->last_error = e.what();
+		return NLI_E_INVALID;
 	}
 	return NLI_OK;
 }
@@ -138,6 +148,12 @@ extern "C" int nli_bruteforce_nnf(nli_ctx *ctx, const nli_distance_params *dist,
 	} catch (const Error &e) {
 		ctx->last_error = e.message;
 		return e.status;
+	} catch (const std::bad_alloc &) {
+		ctx->last_error = "host allocation failed";
+		return NLI_E_NOMEM;
+	} catch (const std::exception &e) {
+		ctx->last_error = e.what();
+		return NLI_E_INVALID;
 	}
 	return NLI_OK;
 }
@@ -161,21 +177,65 @@ namespace nli {
 constexpr size_t kNoAllocScratchFloats = NLI_NOALLOC_SCRATCH_BYTES / sizeof(float);
 static __device__ __align__(256) float g_noalloc_scratch[kNoAllocScratchFloats];
 
-constexpr int kNoAllocMaxDevices = 64;
-static float *g_noalloc_ptr[kNoAllocMaxDevices];
+// The array's device address differs between CUDA contexts: each context
+// (a device's primary context, a context a driver-API host made current,
+// the primary context re-created after cudaDeviceReset) loads the module
+// anew.  So the address is cached per context, keyed by the context's
+// unique ID (cuCtxGetId: never reused within a process, unlike the handle),
+// and looked up once per context with cudaGetSymbolAddress.
+typedef CUresult (*CtxGetCurrentFn)(CUcontext *);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long *);
+
+struct NoAllocEntry {
+	unsigned long long ctx_id;
+	float *ptr;
+};
+static std::vector<NoAllocEntry> g_noalloc_cache;
 static std::mutex g_noalloc_mutex;
 
-// Device address of the scratch array on the current device, looked up
-// once per device (the first call on a device does this set-up).
-static float *noalloc_scratch(int device)
+template <class Fn>
+static Fn driver_fn(const char *name)
+{
+	void *f = nullptr;
+	cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+	if (cudaGetDriverEntryPointByVersion(name, &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+	    q != cudaDriverEntryPointSuccess) {
+		(void)cudaGetLastError();
+		return nullptr;
+	}
+	return reinterpret_cast<Fn>(f);
+}
+
+// ID of the context current on this thread (0 when none is current yet).
+static unsigned long long current_ctx_id()
+{
+	static const CtxGetCurrentFn get_current = driver_fn<CtxGetCurrentFn>("cuCtxGetCurrent");
+	static const CtxGetIdFn get_id = driver_fn<CtxGetIdFn>("cuCtxGetId");
+	NLI_REQUIRE(get_current && get_id, NLI_E_UNSUPPORTED, "the driver lacks cuCtxGetCurrent / cuCtxGetId");
+	CUcontext c = nullptr;
+	if (get_current(&c) != CUDA_SUCCESS || !c) return 0;
+	unsigned long long id = 0;
+	NLI_REQUIRE(get_id(c, &id) == CUDA_SUCCESS, NLI_E_CUDA, "cuCtxGetId failed");
+	return id;
+}
+
+// Device address of the scratch array in the current context.  The first
+// call in a context looks it up (that first call should come before any
+// stream capture); later calls in the same context take it from the cache.
+static float *noalloc_scratch()
 {
 	std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-	if (!g_noalloc_ptr[device]) {
-		float *p = nullptr;
-		NLI_CUDA(cudaGetSymbolAddress((void **)&p, g_noalloc_scratch));
-		g_noalloc_ptr[device] = p;
-	}
-	return g_noalloc_ptr[device];
+	unsigned long long id = current_ctx_id();
+	if (id != 0)
+		for (const NoAllocEntry &e : g_noalloc_cache)
+			if (e.ctx_id == id) return e.ptr;
+	float *p = nullptr;
+	// makes the device's primary context current when none is
+	NLI_CUDA(cudaGetSymbolAddress((void **)&p, g_noalloc_scratch));
+	if (id == 0) id = current_ctx_id();
+	NLI_REQUIRE(id != 0, NLI_E_CUDA, "no CUDA context is current");
+	g_noalloc_cache.push_back({id, p});
+	return p;
 }
 
 }  // namespace nli
@@ -195,10 +255,7 @@ extern "C" int nli_distance_pairs_noalloc(const nli_distance_params *dist, const
 		const size_t gt = (grad && !same) ? (size_t)tW * tH * 2 * C : 0;
 		if (gs + gt > kNoAllocScratchFloats) return NLI_E_INVALID;  // beyond NLI_NOALLOC_SCRATCH_BYTES
 		if (n == 0) return NLI_OK;
-		int device = 0;
-		NLI_CUDA(cudaGetDevice(&device));
-		if (device < 0 || device >= kNoAllocMaxDevices) return NLI_E_UNSUPPORTED;
-		float *scratch = noalloc_scratch(device);
+		float *scratch = noalloc_scratch();
 		cudaStream_t s = (cudaStream_t)stream;
 		const float *grad_s = nullptr, *grad_t = nullptr;
 		if (grad) {
@@ -215,6 +272,10 @@ extern "C" int nli_distance_pairs_noalloc(const nli_distance_params *dist, const
 		NLI_CHECK_LAUNCH();
 	} catch (const Error &e) {
 		return e.status;
+	} catch (const std::bad_alloc &) {
+		return NLI_E_NOMEM;
+	} catch (const std::exception &) {
+		return NLI_E_INVALID;
 	}
 	return NLI_OK;
 }

@@ -492,9 +492,16 @@ Nnf patchmatch_serial(Distance &dist, const nli_patchmatch_params &pm, const Img
 	return nb;
 }
 
-/* PatchMatch::calculate, OpenMP build (patch_match.cpp:65-302).  Not
- * deterministic (thread seeds from time(NULL), :145); used only to time the
- * reference algorithm with all host threads. */
+/* Base of the OpenMP PatchMatch's per-thread seeds when set by
+ * orc_set_parallel_seed (the reference takes time(NULL), :145). */
+bool g_par_seed_set = false;
+unsigned g_par_seed = 0;
+
+/* PatchMatch::calculate, OpenMP build (patch_match.cpp:65-302).  Thread t
+ * draws from rand_r with seed base + t; the reference's base is time(NULL)
+ * (:145), so its runs do not repeat.  With orc_set_parallel_seed and a fixed
+ * thread count the base is fixed and the run repeats (used to make reference
+ * outputs of large images, where the serial variant is too slow). */
 Nnf patchmatch_omp(Distance &dist, const nli_patchmatch_params &pm, const Img &source,
                    const Msk &smask, const Img &target, const Msk &tmask, const Nnf &init)
 {
@@ -536,7 +543,7 @@ Nnf patchmatch_omp(Distance &dist, const nli_patchmatch_params &pm, const Img &s
 		xmax = max(xmax, p.x);
 	}
 	int bbox_w = tp.empty() ? 0 : xmax - xmin + 1;
-	unsigned seed0 = (unsigned)time(NULL);
+	unsigned seed0 = g_par_seed_set ? g_par_seed : (unsigned)time(NULL);
 	int nthreads = 1;
 #ifdef _OPENMP
 	nthreads = omp_get_max_threads();
@@ -1484,6 +1491,21 @@ extern "C" {
 
 const char *orc_last_error(void) { return g_error.c_str(); }
 void orc_srand(unsigned seed) { srand(seed); }
+/* enable != 0: the OpenMP PatchMatch's thread seeds start at `seed` instead
+ * of time(NULL). */
+void orc_set_parallel_seed(int enable, unsigned seed)
+{
+	g_par_seed_set = enable != 0;
+	g_par_seed = seed;
+}
+void orc_set_threads(int n)
+{
+#ifdef _OPENMP
+	if (n > 0) omp_set_num_threads(n);
+#else
+	(void)n;
+#endif
+}
 int orc_max_threads(void)
 {
 #ifdef _OPENMP
@@ -1742,7 +1764,8 @@ float orc_subsampling_rate(float ratio, unsigned scales)
 }
 
 /* ImageInpainting::process after srand(seed); parallel != 0 uses the OpenMP
- * PatchMatch (not repeatable).  stats may be NULL. */
+ * PatchMatch (repeatable only under orc_set_parallel_seed with a fixed
+ * thread count).  stats may be NULL. */
 int orc_process(unsigned seed, int parallel, const nli_process_params *p, const float *img, const uint8_t *mask, int W,
                 int H, int C, float *out, nli_process_stats *stats)
 {

@@ -241,6 +241,19 @@ class Oracle(_Lib):
         self._energy.restype = I
         self._energy.argtypes = [ct.POINTER(_abi.DistanceParams), P, I, I, P, I, I, I, P, P, D]
         self.max_threads = self.lib.orc_max_threads()
+        self.lib.orc_set_parallel_seed.restype = None
+        self.lib.orc_set_parallel_seed.argtypes = [I, ct.c_uint]
+        self.lib.orc_set_threads.restype = None
+        self.lib.orc_set_threads.argtypes = [I]
+
+    def set_parallel_seed(self, seed):
+        """Fixes the base of the OpenMP PatchMatch's thread seeds (None: time(NULL),
+        as the reference)."""
+        self.lib.orc_set_parallel_seed(0 if seed is None else 1, 0 if seed is None else int(seed))
+
+    def set_threads(self, n):
+        self.lib.orc_set_threads(int(n))
+        self.max_threads = self.lib.orc_max_threads()
 
     def nnf_energy(self, dist, src, tgt, tmask, nnf):
         src, tgt, tmask, nnf = _f32(src), _f32(tgt), _u8(tmask), _i32(nnf)

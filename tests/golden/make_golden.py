@@ -4,6 +4,19 @@ oracle/_ref/libnliref.so) on small seeded inputs.
 
     python tests/golden/make_golden.py            # unit + small process cases
     python tests/golden/make_golden.py --full     # full-size configs 1-3 (slow)
+    python tests/golden/make_golden.py --full --seeds 1,2 --skip-units config2
+                                                  # the same configurations for other
+                                                  # input seeds (one file per seed)
+    python tests/golden/make_golden.py --batch 8,15 --skip-units
+                                                  # items of the seeded 64-image uneven
+                                                  # batch (see batch_items)
+
+Full-size configurations run the serial reference build (srand(101)).  The
+uneven-batch items are too large for the serial build (their pyramids have up
+to 16 nearly full-size scales), so they run the pinned restatement with the
+reference's OpenMP PatchMatch (the variant the reference's own Release build
+compiles), its thread seeds fixed by orc_set_parallel_seed and 4 threads, so
+that a rerun reproduces them.
 
 Only runs where the reference sources are present.  The fixtures are
 committed; the tests read them and never need the reference.
@@ -182,28 +195,75 @@ def unit_cases(ref):
     return g
 
 
+# the seeded uneven batch whose items have reference outputs: its seed, size
+# and the parameters of the batch comparison
+BATCH_SEED, BATCH_COUNT, BATCH_MAX_SIDE = 5, 64, 1024
+BATCH_PAR_SEED, BATCH_THREADS = 4242, 4
+
+
+def batch_items(indices):
+    """(index, image, mask, params) of the chosen items of the seeded batch."""
+    items = wl.config5(seed=BATCH_SEED, count=BATCH_COUNT, max_side=BATCH_MAX_SIDE)
+    out = []
+    for i in indices:
+        img, mask, method, scales = items[i]
+        out.append((i, img, mask, wl.config5_params(mask, method, scales)))
+    return out
+
+
+def full_reference_path(name, seed):
+    return os.path.join(HERE, "%s_reference.npz" % name if seed == 0 else "%s_reference_seed%d.npz" % (name, seed))
+
+
+def batch_reference_path(index):
+    return os.path.join(HERE, "batch_reference_%02d.npz" % index)
+
+
+def _arg(flag):
+    return sys.argv[sys.argv.index(flag) + 1] if flag in sys.argv else None
+
+
 def main():
-    oracle_build.build_reference()
-    ref = O.Reference()
-    g = quiet(unit_cases, ref)
-    np.savez_compressed(os.path.join(HERE, "units.npz"), **g)
-    cases = {}
-    for name, img, mask, p in small_configs():
-        out = quiet(ref.process, img, mask, p, seed=101)
-        cases[name + "_img"], cases[name + "_mask"] = img, mask
-        cases[name + "_params"], cases[name + "_out"] = params_to_array(p), out
-    np.savez_compressed(os.path.join(HERE, "process_small.npz"), **cases)
-    if "--full" in sys.argv:
-        full = {}
-        for name, fn in (("config1", lambda: wl.config1(seed=0)), ("config2", lambda: wl.config2(seed=0)),
-                         ("config3", lambda: wl.config3(seed=0))):
-            if len(sys.argv) > 2 and name not in sys.argv:
-                continue
-            img, mask, p = fn()
+    import time
+    names = [a for a in sys.argv[1:] if a.startswith("config")]
+    if "--skip-units" not in sys.argv:
+        oracle_build.build_reference()
+        ref = O.Reference()
+        g = quiet(unit_cases, ref)
+        np.savez_compressed(os.path.join(HERE, "units.npz"), **g)
+        cases = {}
+        for name, img, mask, p in small_configs():
             out = quiet(ref.process, img, mask, p, seed=101)
-            np.savez_compressed(os.path.join(HERE, "%s_reference.npz" % name), hole=out[mask > 0],
-                                params=params_to_array(p), seed=np.array(101))
-            print(name, "done", flush=True)
+            cases[name + "_img"], cases[name + "_mask"] = img, mask
+            cases[name + "_params"], cases[name + "_out"] = params_to_array(p), out
+        np.savez_compressed(os.path.join(HERE, "process_small.npz"), **cases)
+    if "--full" in sys.argv:
+        oracle_build.build_reference()
+        ref = O.Reference()
+        seeds = [int(x) for x in (_arg("--seeds") or "0").split(",")]
+        for seed in seeds:
+            for name, fn in (("config1", lambda: wl.config1(seed=seed)), ("config2", lambda: wl.config2(seed=seed)),
+                             ("config3", lambda: wl.config3(seed=seed))):
+                if names and name not in names:
+                    continue
+                img, mask, p = fn()
+                t0 = time.time()
+                out = quiet(ref.process, img, mask, p, seed=101)
+                np.savez_compressed(full_reference_path(name, seed), hole=out[mask > 0],
+                                    params=params_to_array(p), seed=np.array(101), input_seed=np.array(seed))
+                print(name, "seed", seed, "done in %.0f s" % (time.time() - t0), flush=True)
+    if _arg("--batch"):
+        orc = O.Oracle()
+        orc.set_threads(BATCH_THREADS)
+        orc.set_parallel_seed(BATCH_PAR_SEED)
+        for i, img, mask, p in batch_items([int(x) for x in _arg("--batch").split(",")]):
+            t0 = time.time()
+            out = quiet(orc.process, img, mask, p, seed=101, parallel=True)
+            np.savez_compressed(batch_reference_path(i), hole=out[mask > 0], params=params_to_array(p),
+                                seed=np.array(101), parallel_seed=np.array(BATCH_PAR_SEED),
+                                threads=np.array(BATCH_THREADS), index=np.array(i),
+                                batch=np.array([BATCH_SEED, BATCH_COUNT, BATCH_MAX_SIDE]))
+            print("batch item", i, img.shape, "done in %.0f s" % (time.time() - t0), flush=True)
 
 
 if __name__ == "__main__":
