@@ -67,6 +67,9 @@ PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 # ncu summary of the dominant kernel; its "traffic_bytes_per_launch:" line is
 # the DRAM bytes (read + write) of one finest-scale sweep
 TRAFFIC = os.path.join(ROOT, "profiles", "pm_sweep_l2combined_512x512.md")
+# the CPU baseline's build of the reference algorithm (oracle/build.py)
+TIMING_FLAGS = "g++ -O3 -DNDEBUG -std=gnu++17 -fopenmp (the reference's Release build flags)"
+GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 
 def workload_desc():
@@ -148,7 +151,7 @@ def cpu_sample(img, mask, p, iterations):
     every scale with the oracle restatement and returns (estimated seconds
     of a whole process(), wall seconds spent, threads)."""
     from oracle import oracle as O
-    orc = O.Oracle()
+    orc = O.Oracle(timing=True)
     S = p.scales
     imgs, masks = [np.asarray(img, np.float32)], [np.asarray(mask, np.uint8)]
     for i in range(1, S):
@@ -176,6 +179,26 @@ def cpu_sample(img, mask, p, iterations):
         if lvl < S - 1:  # propagate_weights into this scale: 2 PatchMatch + 1 update
             est += t_pm[lvl + 1] + t_pm[lvl] + t_up[lvl]
     return est, wall, orc.max_threads
+
+
+def cpu_calibration():
+    """Checks the per-scale sampling of cpu_sample against a whole timed
+    process() on the 256x256 NL-means workload: the OpenMP restatement (the
+    reference's Release flags) runs the whole process() once, then the
+    sampled estimate is formed with that run's own per-scale iteration
+    counts.  Returns {measured_s, estimated_s, ratio, ...}."""
+    from oracle import oracle as O
+    from nli_gb300 import workloads as wl
+    orc = O.Oracle(timing=True)
+    img, mask, p = wl.config1(seed=0)
+    orc.process(img[:64, :64].copy(), mask[:64, :64].copy(), p, parallel=True)  # warm the threads
+    t0 = time.perf_counter()
+    _, st = orc.process(img, mask, p, seed=101, parallel=True, return_stats=True)
+    measured = time.perf_counter() - t0
+    est, wall, threads = cpu_sample(img, mask, p, list(st["iterations"][:p.scales]))
+    return {"workload": "256x256 NL-means (nlmeans256), one whole OpenMP process()", "measured_s": measured,
+            "estimated_s": est, "ratio": est / measured, "sample_wall_s": wall, "cores": threads,
+            "iterations": list(st["iterations"][:p.scales])}
 
 
 def max_over_ranks(value, device="cpu"):
@@ -222,6 +245,7 @@ def run_reference(args):
         walls.append(wall)
     est = statistics.median(ests)
     value = mpix / est
+    calib = cpu_calibration()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * statistics.mean(walls), "higher_is_better": True,
@@ -231,7 +255,8 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": "per step: 1 PatchMatch (OpenMP) + 1 NL-Poisson update on each of the 8 scales, "
                                    "scaled by the per-scale call counts of the %s; estimated %.1f s per "
-                                   "process()" % (source, est)},
+                                   "process()" % (source, est),
+                         "flags": TIMING_FLAGS, "calibration": calib},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -391,7 +416,8 @@ def run_ours(args):
         cpu = {"value": mpix / est, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": "1 PatchMatch (OpenMP) + 1 %s update on each of the %d scales (%.1f s wall), scaled "
                          "by the per-scale call counts of the %s: %.1f s per process()"
-                         % (method, p.scales, wall, source, est)}
+                         % (method, p.scales, wall, source, est),
+               "flags": TIMING_FLAGS, "calibration": cpu_calibration()}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -426,14 +452,47 @@ def run_ours(args):
     return 0
 
 
+def hole_psnr(out, truth, mask):
+    """PSNR (peak 255) over the hole pixels and channels."""
+    m = np.asarray(mask) > 0
+    d = np.asarray(out, np.float64)[m] - np.asarray(truth, np.float64)[m]
+    mse = float(np.mean(d * d))
+    return float("inf") if mse == 0 else 10.0 * np.log10(255.0 ** 2 / mse)
+
+
+def batch_reference_gaps(items5, outs):
+    """Hole PSNR against the truth (the input's hole pixels) of our outputs
+    and of the reference's (tests/golden/batch_reference_*.npz, made by
+    tests/golden/make_golden.py --batch) for the batch items that have
+    one; gap = ours - reference (dB)."""
+    import glob
+    rows = []
+    for path in sorted(glob.glob(os.path.join(GOLDEN, "batch_reference_*.npz"))):
+        g = np.load(path)
+        i = int(g["index"])
+        if i >= len(outs) or tuple(g["batch"]) != (5, 64, 1024):
+            continue
+        img, mask = items5[i][0], items5[i][1]
+        truth = img[mask > 0].astype(np.float64)
+        ref = g["hole"].astype(np.float64)
+        p_ref = 10.0 * np.log10(255.0 ** 2 / float(np.mean((ref - truth) ** 2)))
+        p_ours = hole_psnr(outs[i], img, mask)
+        rows.append({"index": i, "size": [int(img.shape[1]), int(img.shape[0])], "method": items5[i][2],
+                     "psnr_ours_db": p_ours, "psnr_reference_db": p_ref, "gap_db": p_ours - p_ref})
+    return rows
+
+
 def batch_compare(pkg, ctx, args, local):
-    """Plain per-image path against the batched path on a seeded batch shaped
-    like the uneven-batch workload: `--batch-count` images, sides
-    log-uniform in [128, --batch-max-side], aspect 0.5-2, 5-30 % ellipse or
-    stroke holes, alternating nlmeans / nlpoisson, patch 9, scales
+    """Plain per-image path against the batched path on the uneven-batch
+    workload: `--batch-count` images (64), sides log-uniform in [128,
+    --batch-max-side (1024)], aspect 0.5-2, 5-30 % ellipse or stroke holes,
+    alternating nlmeans / nlpoisson, patch 9, scales
     |round(log(size 0.1) / log(0.75))| with the automatic coarsest rate.
-    Inputs resident in HBM; each path timed once after one warm-up pass,
-    with CUDA events on the context's stream (the batch joins it)."""
+    Inputs resident in HBM; the batched path (lockstep) runs once untimed
+    (it sizes its workspace) and once timed, the plain path once timed, each
+    with CUDA events on the context's stream.  Outputs are compared bit for
+    bit, and the hole PSNR of the items with a reference output is compared
+    with the reference's."""
     import torch
     from nli_gb300 import workloads as wl
     items5 = wl.config5(seed=5, count=args.batch_count, max_side=args.batch_max_side)
@@ -451,10 +510,14 @@ def batch_compare(pkg, ctx, args, local):
             ctx.set_seed(ctx.batch_seed(seed, i))
             ctx.process_device(im, m, p, out=ref[i])
 
-    def batched():
+    def batched(mode=1):
         ctx.set_seed(seed)
+        ctx.set_tuning(ctx.TUNE_BATCH_MODE, mode)
         ctx.set_batch_width(args.batch_width)
-        ctx.process_batch_device(items, params, outs=outs)
+        try:
+            ctx.process_batch_device(items, params, outs=outs)
+        finally:
+            ctx.set_tuning(ctx.TUNE_BATCH_MODE, 1)
 
     def timed(fn):
         torch.cuda.synchronize()
@@ -465,12 +528,19 @@ def batch_compare(pkg, ctx, args, local):
         torch.cuda.synchronize()
         return a.elapsed_time(b) / 1e3
 
-    l0 = ctx.launch_count()
     batched()
-    launches = ctx.launch_count() - l0
+    l0 = ctx.launch_count()
     tb = timed(batched)
-    plain()
+    launches = ctx.launch_count() - l0
     tp = timed(plain)
+    identical = all(bool(torch.equal(x, y)) for x, y in zip(outs, ref))
+    workers = None
+    if args.batch_workers:
+        batched(0)
+        tw = timed(lambda: batched(0))
+        workers = {"mpix_s": mpix / tw, "s": tw, "batch_width": args.batch_width,
+                   "identical_to_plain": all(bool(torch.equal(x, y)) for x, y in zip(outs, ref)),
+                   "path": "worker contexts (NLI_TUNE_BATCH_MODE 0): whole process() runs on their own streams"}
 
     def kernel_ms(fn):
         # one more pass with per-kernel CUDA events (outside the timed passes)
@@ -481,13 +551,21 @@ def batch_compare(pkg, ctx, args, local):
         return {k: round(v[1], 1) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][1])}
 
     kb, kp = (kernel_ms(batched), kernel_ms(plain)) if args.batch_profile else (None, None)
+    host = [o.cpu().numpy() for o in ref]
+    gaps = batch_reference_gaps(items5, host)
     return {"workload": "uneven batch: %d images, sides log-uniform 128-%d, aspect 0.5-2, 5-30%% ellipse/stroke "
                         "holes, nlmeans/nlpoisson alternating, patch 9, scales |round(log(0.1 size)/log(0.75))|, "
                         "automatic coarsest rate (seed 5)" % (len(items), args.batch_max_side),
             "mpix": mpix, "plain_mpix_s": mpix / tp, "batched_mpix_s": mpix / tb, "speedup": tp / tb,
-            "plain_s": tp, "batched_s": tb, "batch_width": args.batch_width, "gpu_launches": int(launches),
-            "identical_to_plain": all(bool(torch.equal(x, y)) for x, y in zip(outs, ref)),
-            "kernel_ms_plain": kp, "kernel_ms_batched": kb,
+            "plain_s": tp, "batched_s": tb,
+            "batched_path": "lockstep: one launch per kernel per pyramid rank over every image, each rank's "
+                            "iteration loop one CUDA graph (while node, per-image stopping test on the device)",
+            "plain_path": "one process() per image, iterations after a scale's first in one CUDA graph",
+            "gpu_launches": int(launches), "identical_to_plain": identical,
+            "reference_psnr": gaps,
+            "max_psnr_gap_db": max((-r["gap_db"] for r in gaps), default=None),
+            "mean_psnr_gap_db": float(np.mean([r["gap_db"] for r in gaps])) if gaps else None,
+            "workers": workers, "kernel_ms_plain": kp, "kernel_ms_batched": kb,
             "scales": [p.scales for p in params]}
 
 
@@ -551,12 +629,16 @@ def main():
     ap.add_argument("--cg-precond", type=int, default=None, choices=[0, 1],
                     help="NL-Poisson CG: 0 plain (the reference's), 1 Jacobi-preconditioned "
                          "(default: the library's, 0)")
-    ap.add_argument("--batch-count", type=int, default=16,
+    ap.add_argument("--batch-count", type=int, default=64,
                     help="images in the batched-vs-plain comparison (0 skips it)")
-    ap.add_argument("--batch-max-side", type=int, default=512)
-    ap.add_argument("--batch-width", type=int, default=8)
-    ap.add_argument("--no-batch-profile", dest="batch_profile", action="store_false",
-                    help="skip the per-kernel profiled passes of the batch comparison")
+    ap.add_argument("--batch-max-side", type=int, default=1024)
+    ap.add_argument("--batch-width", type=int, default=8,
+                    help="images in flight in the worker-context batch form")
+    ap.add_argument("--batch-profile", action="store_true",
+                    help="add per-kernel profiled passes of both paths to the batch comparison")
+    ap.add_argument("--no-batch-profile", dest="batch_profile", action="store_false")
+    ap.add_argument("--batch-workers", action="store_true",
+                    help="also time the worker-context batch form (NLI_TUNE_BATCH_MODE 0)")
     args = ap.parse_args()
     global WORKLOAD
     WORKLOAD = args.workload

@@ -426,6 +426,18 @@ int nli_ctx_set_batch_width(nli_ctx *ctx, int width);
  *                                  batches too.  0: the host loop everywhere.
  *                                  Identical results; the graph is not used
  *                                  while profiling is on.
+ *   NLI_TUNE_CG_SINGLE_MAX         CG systems (per channel) of at most this
+ *                                  many unknowns are solved by one CTA with
+ *                                  block barriers only, instead of a cluster
+ *                                  (0..4096, default 1024).
+ *   NLI_TUNE_BATCH_MODE            how nli_process_batch(_device) runs a
+ *                                  batch: 1 (default) lockstep -- the images
+ *                                  walk their pyramids together, one launch
+ *                                  per kernel per pyramid rank covers every
+ *                                  image, and each rank's iteration loop is
+ *                                  one CUDA graph; 0 worker contexts -- up to
+ *                                  the batch width of whole nli_process runs
+ *                                  on their own streams.  Identical results.
  * nli_ctx_get_tuning reads them back. */
 #define NLI_TUNE_CG_CLUSTER_CAP 0
 #define NLI_TUNE_CG_UNKNOWNS_PER_CTA 1
@@ -433,6 +445,8 @@ int nli_ctx_set_batch_width(nli_ctx *ctx, int width);
 #define NLI_TUNE_PM_VARIANT 3
 #define NLI_TUNE_CG_PRECOND 4
 #define NLI_TUNE_GRAPH_LOOP 5
+#define NLI_TUNE_CG_SINGLE_MAX 6
+#define NLI_TUNE_BATCH_MODE 7
 int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value);
 int nli_ctx_get_tuning(nli_ctx *ctx, int knob, int *value);
 /* The seed image `index` of a batch runs with. */
@@ -444,6 +458,21 @@ uint64_t nli_batch_seed(uint64_t seed, int index);
  * throw std::bad_alloc); this one checks that a failed call leaves the
  * context usable. */
 int nli_debug_fail_allocation(nli_ctx *ctx, int countdown);
+/* Test hook for the bounded device waits: the grid CG's grid barrier gives
+ * up after `polls` polls (0 restores the default, 2^26).  A wait that runs
+ * out sets the context's timeout word, every block of the kernel leaves,
+ * and the call returns NLI_E_TIMEOUT ("a device-side wait timed out"); the
+ * word is then cleared, so the context stays usable.  The reference has no
+ * device waits; this checks the recovery path without hanging a GPU. */
+int nli_debug_grid_wait_limit(nli_ctx *ctx, unsigned int polls);
+/* Checked builds (libnli_gb300_checked.so, built with NLI_CHECKED): every
+ * data-dependent gathered index -- source pixels of PatchMatch candidates,
+ * NNF-shifted pixels of the updates, hole lists, CG neighbour codes -- is
+ * tested against its buffer; the first out-of-range one is recorded as
+ * (site << 32) | (index & 0xffffffff) and its access is skipped.  Reads and
+ * clears that record into *word (0: none).  *checked is 1 in checked
+ * builds, 0 otherwise (where *word is always 0). */
+int nli_debug_check_status(nli_ctx *ctx, unsigned long long *word, int *checked);
 
 #ifdef __cplusplus
 }

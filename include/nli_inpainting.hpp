@@ -12,8 +12,10 @@
  * include/nli_dropin/ carry the reference's header names.  Every
  * computation runs on the GPU through nli.h; there is no CPU path.
  *
- * The containers are the subset of the reference's Image / Mask / Point /
- * Shape API that this interface and its callers use, with the same
+ * The containers carry the reference's Image / Mask / Point / Shape API
+ * that this interface and host code like its callers use (Mask and
+ * FixedMask in full: iterators, channel overloads, at(), first / last /
+ * next / prev, bounding box, clone / clone_invert), with the same
  * semantics: copying an Image or Mask shares its buffer (image.hpp:93-112,
  * 555-558), constructing an Image from a FixedImage or a Mask from a
  * FixedMask copies it (image.hpp:561-577, mask.cpp:559-563), pixels are
@@ -135,9 +137,52 @@ public:
 };
 
 /* ----------------------------------------------------------------- mask.h */
-/* One byte per pixel (the reference stores bool per pixel, mask.h). */
+/* A flag per pixel (bool, as the reference stores them, mask.h), shared
+ * between copies like an Image's buffer.  Iteration visits the set pixels
+ * in raster order (mask.cpp:158-179, 332-381; mask_iterator.cpp). */
+class FixedMask;
+
+class MaskIterator {
+public:
+	typedef const Point &const_reference;
+	typedef const Point *const_pointer;
+	MaskIterator() : _mask(nullptr), _current(-1, -1), _reverse(false) {}
+	MaskIterator(const FixedMask *mask, Point current, bool reverse = false)
+	    : _mask(mask), _current(current), _reverse(reverse)
+	{
+	}
+	bool operator==(const MaskIterator &o) const
+	{
+		return _mask == o._mask && _current == o._current && _reverse == o._reverse;
+	}
+	bool operator!=(const MaskIterator &o) const { return !(*this == o); }
+	inline MaskIterator &operator++();
+	inline MaskIterator &operator--();
+	MaskIterator operator++(int)
+	{
+		MaskIterator before(*this);
+		++*this;
+		return before;
+	}
+	MaskIterator operator--(int)
+	{
+		MaskIterator before(*this);
+		--*this;
+		return before;
+	}
+	const_reference operator*() const { return _current; }
+	const_pointer operator->() const { return &_current; }
+
+private:
+	const FixedMask *_mask;
+	Point _current;
+	bool _reverse;
+};
+
 class FixedMask {
 public:
+	typedef MaskIterator iterator;
+
 	FixedMask() : _sx(0), _sy(0) {}
 	FixedMask(uint sx, uint sy) { init(sx, sy, false); }
 	FixedMask(uint sx, uint sy, bool v) { init(sx, sy, v); }
@@ -149,68 +194,207 @@ public:
 	uint get_size_y() const { return _sy; }
 	uint get_number_of_channels() const { return 1; }
 	Shape get_size() const { return Shape(_sx, _sy); }
-	bool is_empty() const { return !_d || _d->empty(); }
+	bool is_empty() const { return !_d || count() == 0; }
 	bool is_not_empty() const { return !is_empty(); }
-	bool operator()(uint x, uint y) const { return (*_d)[(size_t)y * _sx + x] != 0; }
+
+	/* raster order; end() is Point(size_x, size_y), rend() Point(-1, -1) */
+	iterator begin() const { return iterator(this, first()); }
+	iterator end() const { return iterator(this, Point((int)_sx, (int)_sy)); }
+	iterator rbegin() const { return iterator(this, last(), true); }
+	iterator rend() const { return iterator(this, Point(-1, -1), true); }
+
+	/* without range checking */
+	bool operator()(uint x, uint y) const { return _d.get()[index(x, y, 0)]; }
 	bool operator()(Point p) const { return (*this)((uint)p.x, (uint)p.y); }
-	bool get(uint x, uint y) const { return (*this)(x, y); }
-	bool get(Point p) const { return (*this)(p); }
-	/* false outside the image (mask.cpp:223-272) */
-	bool test(uint x, uint y) const { return x < _sx && y < _sy && (*this)(x, y); }
+	bool get(uint x, uint y) const { return _d.get()[index(x, y, 0)]; }
+	bool get(uint x, uint y, uint channel) const { return _d.get()[index(x, y, channel)]; }
+	bool get(Point p) const { return get((uint)p.x, (uint)p.y); }
+	bool get(Point p, uint channel) const { return get((uint)p.x, (uint)p.y, channel); }
+	/* false outside the image or beyond the one channel (mask.cpp:223-272) */
+	bool test(uint x, uint y) const { return x < _sx && y < _sy && get(x, y); }
+	bool test(uint x, uint y, uint channel) const { return channel == 0 && test(x, y); }
 	bool test(Point p) const { return p.x >= 0 && p.y >= 0 && test((uint)p.x, (uint)p.y); }
+	bool test(Point p, uint channel) const { return channel == 0 && test(p); }
+
+	/* deep copies; clone_invert flips every flag */
+	FixedMask clone() const
+	{
+		FixedMask c;
+		c.copy_from(*this, false);
+		return c;
+	}
+	FixedMask clone_invert() const
+	{
+		FixedMask c;
+		c.copy_from(*this, true);
+		return c;
+	}
+
 	/* raster order (mask.cpp:378-390) */
 	std::vector<Point> get_masked_points() const
 	{
 		std::vector<Point> v;
-		for (uint y = 0; y < _sy; y++)
-			for (uint x = 0; x < _sx; x++)
-				if ((*this)(x, y)) v.push_back(Point(x, y));
+		for (iterator it = begin(); it != end(); ++it) v.push_back(*it);
 		return v;
 	}
-	/* bytes 0/1, row-major, as the C ABI takes them */
-	const uint8_t *bytes() const { return _d ? _d->data() : nullptr; }
+
+	/* the first / last set pixel in raster order: Point(size_x, size_y) /
+	 * Point(-1, -1) when none is set (mask.cpp:332-349, 425-454) */
+	Point first() const
+	{
+		for (uint y = 0; y < _sy; y++)
+			for (uint x = 0; x < _sx; x++)
+				if (get(x, y)) return Point((int)x, (int)y);
+		return Point((int)_sx, (int)_sy);
+	}
+	Point last() const
+	{
+		for (int y = (int)_sy - 1; y >= 0; y--)
+			for (int x = (int)_sx - 1; x >= 0; x--)
+				if (get((uint)x, (uint)y)) return Point(x, y);
+		return Point(-1, -1);
+	}
+	/* the next / previous set pixel after / before `current` in raster
+	 * order, else Point(size_x, size_y) / Point(-1, -1) (mask.cpp:352-381);
+	 * from rend() / end() they start at the first / last pixel */
+	Point next(const Point &current) const
+	{
+		int y = current.y, x0 = current.x + 1;
+		if (y < 0) y = x0 = 0;
+		for (; y < (int)_sy; y++, x0 = 0)
+			for (int x = std::max(x0, 0); x < (int)_sx; x++)
+				if (get((uint)x, (uint)y)) return Point(x, y);
+		return Point((int)_sx, (int)_sy);
+	}
+	Point prev(const Point &current) const
+	{
+		int y = current.y, x0 = current.x - 1;
+		if (y >= (int)_sy) {
+			y = (int)_sy - 1;
+			x0 = (int)_sx - 1;
+		}
+		for (; y >= 0; y--, x0 = (int)_sx - 1)
+			for (int x = std::min(x0, (int)_sx - 1); x >= 0; x--)
+				if (get((uint)x, (uint)y)) return Point(x, y);
+		return Point(-1, -1);
+	}
+	/* corners of the smallest rectangle holding every set pixel, both
+	 * Point(-1, -1) when none is set (mask.cpp:384-401, 460-486) */
+	Point bounding_box_top_left() const { return bounding_box(true); }
+	Point bounding_box_bottom_right() const { return bounding_box(false); }
+
+	/* flags as bytes 0/1, row-major, as the C ABI takes them */
+	const uint8_t *bytes() const { return reinterpret_cast<const uint8_t *>(_d.get()); }
 
 protected:
 	uint _sx, _sy;
-	std::shared_ptr<std::vector<uint8_t>> _d;
+	std::shared_ptr<bool> _d;
+	size_t count() const { return (size_t)_sx * _sy; }
+	size_t index(uint x, uint y, uint channel) const { return (size_t)_sx * y + x + channel; }
 	void init(uint sx, uint sy, bool v)
 	{
 		_sx = sx;
 		_sy = sy;
-		_d = std::make_shared<std::vector<uint8_t>>((size_t)sx * sy, v ? 1 : 0);
+		_d = std::shared_ptr<bool>(new bool[std::max<size_t>(count(), 1)], std::default_delete<bool[]>());
+		std::fill(_d.get(), _d.get() + count(), v);
+	}
+	void copy_from(const FixedMask &o, bool invert)
+	{
+		_sx = o._sx;
+		_sy = o._sy;
+		_d.reset();
+		if (!o._d) return;
+		init(o._sx, o._sy, false);
+		for (size_t i = 0; i < count(); i++) _d.get()[i] = invert ? !o._d.get()[i] : o._d.get()[i];
+	}
+	Point bounding_box(bool top_left) const
+	{
+		int x0 = (int)_sx, y0 = (int)_sy, x1 = -1, y1 = -1;
+		for (uint y = 0; y < _sy; y++)
+			for (uint x = 0; x < _sx; x++)
+				if (get(x, y)) {
+					x0 = std::min(x0, (int)x);
+					y0 = std::min(y0, (int)y);
+					x1 = std::max(x1, (int)x);
+					y1 = std::max(y1, (int)y);
+				}
+		if (x1 < 0) return Point(-1, -1);
+		return top_left ? Point(x0, y0) : Point(x1, y1);
 	}
 	friend class Mask;
 };
 
+MaskIterator &MaskIterator::operator++()
+{
+	if (_mask) _current = _reverse ? _mask->prev(_current) : _mask->next(_current);
+	return *this;
+}
+
+MaskIterator &MaskIterator::operator--()
+{
+	if (_mask) _current = _reverse ? _mask->next(_current) : _mask->prev(_current);
+	return *this;
+}
+
 class Mask : public FixedMask {
 public:
+	typedef MaskIterator iterator;
+
 	Mask() {}
 	Mask(uint sx, uint sy) : FixedMask(sx, sy) {}
 	Mask(uint sx, uint sy, bool v) : FixedMask(sx, sy, v) {}
 	Mask(Shape s) : FixedMask(s) {}
 	Mask(Shape s, bool v) : FixedMask(s, v) {}
-	Mask(const Mask &o) : FixedMask(o) {}  // shares the buffer
-	Mask(const FixedMask &o) : FixedMask(o)  // deep copy
-	{
-		if (o._d) _d = std::make_shared<std::vector<uint8_t>>(*o._d);
-	}
+	Mask(const Mask &o) : FixedMask(o) {}  // shares the flags
+	Mask(const FixedMask &o) { copy_from(o, false); }  // deep copy
 	Mask &operator=(const Mask &o)
 	{
 		FixedMask::operator=(o);
 		return *this;
 	}
-	/* set / clear with range checking (does nothing out of range) */
-	void mask(uint x, uint y)
+	Mask &operator=(const FixedMask &o)  // deep copy
 	{
-		if (x < _sx && y < _sy) (*_d)[(size_t)y * _sx + x] = 1;
+		if (&o != this) copy_from(o, false);
+		return *this;
 	}
-	void unmask(uint x, uint y)
+
+	/* without range checking */
+	using FixedMask::operator();
+	bool &operator()(uint x, uint y) { return _d.get()[index(x, y, 0)]; }
+	bool &operator()(uint x, uint y, uint channel) { return _d.get()[index(x, y, channel)]; }
+	bool &operator()(Point p) { return (*this)((uint)p.x, (uint)p.y); }
+	bool &operator()(Point p, uint channel) { return (*this)((uint)p.x, (uint)p.y, channel); }
+	/* with range checking: std::out_of_range outside the image or beyond
+	 * the one channel */
+	bool &at(uint x, uint y) { return at(x, y, 0u); }
+	bool &at(uint x, uint y, uint channel)
 	{
-		if (x < _sx && y < _sy) (*_d)[(size_t)y * _sx + x] = 0;
+		if (x >= _sx || y >= _sy || channel != 0) throw std::out_of_range("Mask::at: position out of range");
+		return _d.get()[index(x, y, channel)];
 	}
+	bool &at(Point p) { return at(p, 0u); }
+	bool &at(Point p, uint channel)
+	{
+		if (p.x < 0 || p.y < 0) throw std::out_of_range("Mask::at: position out of range");
+		return at((uint)p.x, (uint)p.y, channel);
+	}
+
+	/* set / clear with range checking (nothing happens out of range).
+	 * Every unmask overload clears: the reference's unmask(x, y, channel),
+	 * unmask(Point) and unmask(Point, channel) set the flag instead
+	 * (mask.cpp:844-878), which no caller on the inpainting path reaches. */
+	void mask(uint x, uint y) { set(x, y, 0, true); }
+	void mask(uint x, uint y, uint channel) { set(x, y, channel, true); }
+	void mask(Point p) { set(p, 0, true); }
+	void mask(Point p, uint channel) { set(p, channel, true); }
+	void unmask(uint x, uint y) { set(x, y, 0, false); }
+	void unmask(uint x, uint y, uint channel) { set(x, y, channel, false); }
+	void unmask(Point p) { set(p, 0, false); }
+	void unmask(Point p, uint channel) { set(p, channel, false); }
+
 	void invert()
 	{
-		for (auto &b : *_d) b = b ? 0 : 1;
+		for (size_t i = 0; i < count(); i++) _d.get()[i] = !_d.get()[i];
 	}
 	Mask clone() const { return Mask(static_cast<const FixedMask &>(*this)); }
 	Mask clone_invert() const
@@ -218,6 +402,16 @@ public:
 		Mask m = clone();
 		m.invert();
 		return m;
+	}
+
+private:
+	void set(uint x, uint y, uint channel, bool v)
+	{
+		if (x < _sx && y < _sy && channel == 0) _d.get()[index(x, y, 0)] = v;
+	}
+	void set(Point p, uint channel, bool v)
+	{
+		if (p.x >= 0 && p.y >= 0) set((uint)p.x, (uint)p.y, channel, v);
 	}
 };
 

@@ -23,6 +23,10 @@ LIB_PATH = os.path.join(HERE, "libnli_gb300.so")
 HEADER = os.path.join(os.path.dirname(HERE), "include", "nli.h")
 
 _lib = None
+_libs = {}
+# the checked build (NLI_CHECKED: bounds tests on gathered indices), built on
+# demand by build.build(checked=True)
+CHECKED_LIB_PATH = os.path.join(HERE, "libnli_gb300_checked.so")
 
 P = ct.c_void_p
 I = ct.c_int
@@ -49,12 +53,13 @@ def exported_symbols():
 
 
 def load(path=LIB_PATH):
-    """Loads libnli_gb300.so (raises if it was not built)."""
+    """Loads libnli_gb300.so, or another build of it at `path` (raises if
+    it was not built)."""
     global _lib
-    if _lib is not None:
-        return _lib
+    if path in _libs:
+        return _libs[path]
     if not os.path.exists(path):
-        raise ImportError("libnli_gb300.so not found at %s: run __graft_entry__.build()" % path)
+        raise ImportError("%s not found: run __graft_entry__.build()" % path)
     L = ct.CDLL(path)
 
     def proto(name, res, args):
@@ -105,6 +110,8 @@ def load(path=LIB_PATH):
     proto("nli_ctx_set_batch_width", I, [P, I])
     proto("nli_batch_seed", ct.c_uint64, [ct.c_uint64, I])
     proto("nli_debug_fail_allocation", I, [P, I])
+    proto("nli_debug_grid_wait_limit", I, [P, ct.c_uint])
+    proto("nli_debug_check_status", I, [P, ct.POINTER(ct.c_ulonglong), ct.POINTER(I)])
     proto("nli_ctx_set_tuning", I, [P, I, I])
     proto("nli_ctx_get_tuning", I, [P, I, ct.POINTER(I)])
     proto("nli_launch_count", ct.c_int64, [])
@@ -112,7 +119,9 @@ def load(path=LIB_PATH):
     proto("nli_ctx_profile_entry", I, [P, I, ct.c_char_p, I, ct.POINTER(ct.c_int64), ct.POINTER(ct.c_double)])
     proto("nli_ctx_counters", I, [P, ct.POINTER(ct.c_int64), ct.POINTER(ct.c_int64), ct.POINTER(ct.c_int64),
                                   ct.POINTER(ct.c_int64)])
-    _lib = L
+    _libs[path] = L
+    if path == LIB_PATH:
+        _lib = L
     return L
 
 
@@ -133,10 +142,10 @@ class Context:
     """One nli_ctx: a CUDA device, a stream, the PatchMatch seed and the
     device workspace.  Not thread-safe (one per host thread)."""
 
-    def __init__(self, device=0):
+    def __init__(self, device=0, lib_path=LIB_PATH):
         import torch
         self.torch = torch
-        self.lib = load()
+        self.lib = load(lib_path)
         self.device = device
         torch.cuda.init()
         h = ct.c_void_p()
@@ -482,6 +491,7 @@ class Context:
         return outs, [s.as_dict() for s in st]
 
     TUNE_CG_CLUSTER_CAP, TUNE_CG_UNKNOWNS_PER_CTA, TUNE_BATCH_WIDTH, TUNE_PM_VARIANT, TUNE_CG_PRECOND, TUNE_GRAPH_LOOP = 0, 1, 2, 3, 4, 5
+    TUNE_CG_SINGLE_MAX, TUNE_BATCH_MODE = 6, 7
 
     def set_tuning(self, knob, value):
         self._check(self.lib.nli_ctx_set_tuning(self.h, knob, value))
@@ -498,6 +508,18 @@ class Context:
         """Test hook: the countdown-th next workspace growth fails with
         NLI_E_NOMEM (nli_debug_fail_allocation); 0 disarms."""
         self._check(self.lib.nli_debug_fail_allocation(self.h, countdown))
+
+    def grid_wait_limit(self, polls):
+        """Test hook: the grid CG's barrier gives up after `polls` polls
+        (nli_debug_grid_wait_limit); 0 restores the default."""
+        self._check(self.lib.nli_debug_grid_wait_limit(self.h, polls))
+
+    def check_status(self):
+        """(word, checked) of nli_debug_check_status: the first out-of-range
+        gathered index of a checked build ((site << 32) | index), cleared."""
+        w, c = ct.c_ulonglong(), I()
+        self._check(self.lib.nli_debug_check_status(self.h, ct.byref(w), ct.byref(c)))
+        return int(w.value), bool(c.value)
 
     def process_device(self, img, mask, params, out=None):
         """ImageInpainting::process on device tensors; returns (out, stats)."""

@@ -42,7 +42,23 @@ def _stale(target, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force=False, verbose=False, extra=()):
+def build(force=False, verbose=False, extra=(), checked=False):
+    """Compiles libnli_gb300.so (and the drop-in library and the command-line
+    program); checked=True instead compiles libnli_gb300_checked.so with
+    NLI_CHECKED, the build whose kernels bounds-test every gathered index."""
+    if checked:
+        return _build_lib(os.path.join(OBJ, "checked"), LIB_CHECKED, force, verbose, list(extra) + ["-DNLI_CHECKED"])
+    _build_lib(OBJ, LIB, force, verbose, extra)
+    build_dropin(force)
+    build_cli(force)
+    return LIB
+
+
+LIB_CHECKED = os.path.join(HERE, "libnli_gb300_checked.so")
+
+
+def _build_lib(objdir, lib, force, verbose, extra):
+    OBJ = objdir
     os.makedirs(OBJ, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(ROOT, "include", "nli.h"))
@@ -62,12 +78,10 @@ def build(force=False, verbose=False, extra=()):
     if verbose:
         for o in outs:
             print(o)
-    if force or jobs or _stale(LIB, objs):
-        _run([nvcc, *ARCH, "-shared", *objs, "-o", LIB + ".tmp", "-lcudart"])
-        os.replace(LIB + ".tmp", LIB)
-    build_dropin(force)
-    build_cli(force)
-    return LIB
+    if force or jobs or _stale(lib, objs):
+        _run([nvcc, *ARCH, "-shared", *objs, "-o", lib + ".tmp", "-lcudart"])
+        os.replace(lib + ".tmp", lib)
+    return lib
 
 
 def build_dropin(force=False):

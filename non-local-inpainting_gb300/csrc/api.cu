@@ -594,6 +594,30 @@ int nli_debug_fail_allocation(nli_ctx *ctx, int countdown)
 	return NLI_OK;
 }
 
+int nli_debug_grid_wait_limit(nli_ctx *ctx, unsigned int polls)
+{
+	API_BEGIN(ctx)
+	NLI_CUDA(cudaMemcpyAsync(&ctx->status->wait_limit, &polls, sizeof(polls), cudaMemcpyHostToDevice, ctx->stream));
+	NLI_CUDA(cudaStreamSynchronize(ctx->stream));
+	API_END(ctx)
+}
+
+int nli_debug_check_status(nli_ctx *ctx, unsigned long long *word, int *checked)
+{
+	API_BEGIN(ctx)
+	require_ptrs({word, checked});
+	NLI_CUDA(cudaStreamSynchronize(ctx->stream));
+	*word = 0;
+	for (unsigned long long w : {check_word_patchmatch(), check_word_update(), check_word_process()})
+		if (!*word) *word = w;
+#ifdef NLI_CHECKED
+	*checked = 1;
+#else
+	*checked = 0;
+#endif
+	API_END(ctx)
+}
+
 int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value)
 {
 	if (!ctx) return NLI_E_INVALID;
@@ -622,6 +646,14 @@ int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value)
 		if (value < 0 || value > 2) return NLI_E_INVALID;
 		ctx->tune_graph_loop = value;
 		return NLI_OK;
+	case NLI_TUNE_CG_SINGLE_MAX:
+		if (value < 0 || value > 4096) return NLI_E_INVALID;
+		ctx->tune_cg_single_max = value;
+		return NLI_OK;
+	case NLI_TUNE_BATCH_MODE:
+		if (value != 0 && value != 1) return NLI_E_INVALID;
+		ctx->tune_batch_mode = value;
+		return NLI_OK;
 	}
 	return NLI_E_INVALID;
 }
@@ -636,6 +668,8 @@ int nli_ctx_get_tuning(nli_ctx *ctx, int knob, int *value)
 	case NLI_TUNE_PM_VARIANT: *value = ctx->tune_pm_variant; return NLI_OK;
 	case NLI_TUNE_CG_PRECOND: *value = ctx->tune_cg_precond; return NLI_OK;
 	case NLI_TUNE_GRAPH_LOOP: *value = ctx->tune_graph_loop; return NLI_OK;
+	case NLI_TUNE_CG_SINGLE_MAX: *value = ctx->tune_cg_single_max; return NLI_OK;
+	case NLI_TUNE_BATCH_MODE: *value = ctx->tune_batch_mode; return NLI_OK;
 	}
 	return NLI_E_INVALID;
 }

@@ -59,6 +59,11 @@ void process_batch_run(nli_ctx *ctx, int n, const nli_process_params *params, co
                        bool host_buffers)
 {
 	if (n <= 0) return;
+	if (ctx->tune_batch_mode == 1) {
+		lockstep_batch_run(ctx, n, params, images, masks, widths, heights, channels, outputs, stats, status,
+		                   host_buffers);
+		return;
+	}
 	const int width = std::max(1, std::min(ctx->batch_width, n));
 	while ((int)ctx->workers.size() < width) ctx->workers.push_back(new_worker(ctx->device));
 

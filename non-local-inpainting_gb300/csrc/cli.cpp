@@ -27,6 +27,10 @@
 #include <cstdlib>
 #include <cstring>
 #include <ctime>
+#include <map>
+#include <memory>
+#include <stdexcept>
+#include <utility>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -35,24 +39,6 @@
 #include "png_codec.h"
 
 namespace {
-
-// main.cpp:43-58: removes "-name value" (or "-name" when default_value is
-// NULL) from argv and returns the value.
-const char *pick_option(int *c, char ***v, const char *name, const char *default_value)
-{
-	int argc = *c;
-	char **argv = *v;
-	int id = default_value ? 1 : 0;
-	for (int i = 0; i < argc - id; i++) {
-		if (argv[i][0] == '-' && 0 == strcmp(argv[i] + 1, name)) {
-			char *r = argv[i + id] + 1 - id;
-			*c -= (id + 1);
-			for (int j = i; j < argc - id; j++) (*v)[j] = (*v)[j + id + 1];
-			return r;
-		}
-	}
-	return default_value;
-}
 
 // ----------------------------------------------------------- image files
 // Samples as iio holds them: PNM and PFM are read into floats, PNG into
@@ -309,189 +295,328 @@ float max_hole_distance(const Mask &mask)
 	return mx;
 }
 
-int run(int argc, char *argv[])
+// ---------------------------------------------------------- command line
+// The program's options: the reference's names and defaults (main.cpp:68-82)
+// and -seed.  The accepted syntax is the reference's: "-name value" pairs
+// anywhere on the line, every other word a positional argument, in order.
+struct OptionSpec {
+	const char *name;
+	const char *default_value;
+	const char *help;  // printf format of the usage line; %s is the default
+};
+
+const OptionSpec kOptions[] = {
+    {"method", "nlmeans", " -method \tmethod name [nlmeans/nlmedians/nlpoisson/nldepth] (%s)"},
+    {"patch", "7", " -patch  \tpatch side (%s)"},
+    {"iters", "200", " -iters  \tinpainting iterations (%s)"},
+    {"scales", "11", " -scales \tscales amount (%s)"},
+    {"coarse", "0.1", " -coarse \tcoarsest rate (%s)"},
+    {"conft", "5.0", " -conft  \tconfidence decay time (%s)"},
+    {"confa", "0.1", " -confa  \tconfidence asymptotic value (%s)"},
+    {"lambda", "0.05", " -lambda \tlambda (%s)"},
+    {"init", "poisson", " -init   \tinitialization type [poisson/black/avg/none] (%s)"},
+    {"psigma", "10000.0", " -psigma \tGaussian patch weights (%s)"},
+    {"showpyr", "", " -showpyr\tPREFIX write intermediate pyramid results%s"},
+    {"shownnf", "", " -shownnf\tFILENAME write illustration of the final NNF%s"},
+    {"depth", "", " -depth  \tFILENAME depth map (nldepth)%s"},
+    {"lambdar", "0.05", " -lambdar\tlambda of the colour channels, nldepth (%s)"},
+    {"lambdad", "0.05", " -lambdad\tlambda of the depth channel, nldepth (%s)"},
+    {"seed", "", " -seed   \tN random seed (default: time)%s"},
+};
+
+const OptionSpec *find_option(const char *word)
 {
-	int patch_side = atoi(pick_option(&argc, &argv, "patch", "7"));
-	int inpainting_iterations = atoi(pick_option(&argc, &argv, "iters", "200"));
-	std::string method_name = pick_option(&argc, &argv, "method", "nlmeans");
-	int scales_amount = atoi(pick_option(&argc, &argv, "scales", "11"));
-	float coarsest_rate = atof(pick_option(&argc, &argv, "coarse", "0.1"));
-	float confidence_decay_time = atof(pick_option(&argc, &argv, "conft", "5.0"));
-	float confidence_asymptotic_value = atof(pick_option(&argc, &argv, "confa", "0.1"));
-	float lambda = atof(pick_option(&argc, &argv, "lambda", "0.05"));
-	std::string initialization_type_name = pick_option(&argc, &argv, "init", "poisson");
-	float patch_sigma = atof(pick_option(&argc, &argv, "psigma", "10000.0"));
-	std::string show_nnf_file = pick_option(&argc, &argv, "shownnf", "");
-	std::string show_pyramid_file = pick_option(&argc, &argv, "showpyr", "");
-	std::string depth_name = pick_option(&argc, &argv, "depth", "");
-	float lambda_rgb = atof(pick_option(&argc, &argv, "lambdar", "0.05"));
-	float lambda_d = atof(pick_option(&argc, &argv, "lambdad", "0.05"));
-	const char *seed_opt = pick_option(&argc, &argv, "seed", "");
-	if (argc < 4) {
-		fprintf(stderr, "USAGE:\n%s input mask output [OPTIONS]\n\n", argv[0]);
-		fprintf(stderr, "Available options are:\n");
-		fprintf(stderr, " -method \tmethod name [nlmeans/nlmedians/nlpoisson/nldepth] (%s)\n", method_name.c_str());
-		fprintf(stderr, " -patch  \tpatch side (%d)\n", patch_side);
-		fprintf(stderr, " -iters  \tinpainting iterations (%d)\n", inpainting_iterations);
-		fprintf(stderr, " -scales \tscales amount (%d)\n", scales_amount);
-		fprintf(stderr, " -coarse \tcoarsest rate (%g)\n", coarsest_rate);
-		fprintf(stderr, " -conft  \tconfidence decay time (%g)\n", confidence_decay_time);
-		fprintf(stderr, " -confa  \tconfidence asymptotic value (%g)\n", confidence_asymptotic_value);
-		fprintf(stderr, " -lambda \tlambda (%g)\n", lambda);
-		fprintf(stderr, " -init   \tinitialization type [poisson/black/avg/none] (%s)\n",
-		        initialization_type_name.c_str());
-		fprintf(stderr, " -psigma \tGaussian patch weights (%g)\n", patch_sigma);
-		fprintf(stderr, " -showpyr\tPREFIX write intermediate pyramid results\n");
-		fprintf(stderr, " -shownnf\tFILENAME write illustration of the final NNF\n");
-		fprintf(stderr, " -depth  \tFILENAME depth map (nldepth); -lambdar, -lambdad its lambdas\n");
-		fprintf(stderr, " -seed   \tN random seed (default: time)\n");
-		return 1;
-	}
-	const std::string input_name = argv[1], mask_name = argv[2], output_name = argv[3];
+	if (word[0] != '-') return nullptr;
+	for (const OptionSpec &o : kOptions)
+		if (strcmp(word + 1, o.name) == 0) return &o;
+	return nullptr;
+}
 
-	Image<float> input = convert(rgb_image(read_image(input_name)), true);
-	Image<float> mask_image = mono_image(read_image(mask_name), mask_name);
-	if (input.get_size_x() != mask_image.get_size_x() || input.get_size_y() != mask_image.get_size_y())
-		throw std::runtime_error("ERROR: Input image and mask should be of the same size");
-	bool is_mask_empty = true;
-	Mask mask(mask_image.get_size_x(), mask_image.get_size_y());
-	for (uint y = 0; y < mask_image.get_size_y(); y++)
-		for (uint x = 0; x < mask_image.get_size_x(); x++)
-			if (mask_image.raw()[(size_t)y * mask_image.get_size_x() + x] > 0) {
-				mask.mask(x, y);
-				is_mask_empty = false;
+class CommandLine {
+  public:
+	CommandLine(int argc, char **argv) : program_(argc > 0 ? argv[0] : "nli_inpaint")
+	{
+		for (int i = 1; i < argc; i++) {
+			const OptionSpec *o = find_option(argv[i]);
+			if (!o) {
+				positional_.push_back(argv[i]);
+				continue;
 			}
-	if (is_mask_empty) throw std::runtime_error("ERROR: Mask should not be empty (all black)");
-
-	bool depth_exists = false;
-	if (!depth_name.empty()) {
-		depth_exists = true;
-		Image<float> depth = mono_image(read_image(depth_name), depth_name);
-		if (depth.get_size_x() != input.get_size_x() || depth.get_size_y() != input.get_size_y())
-			throw std::runtime_error("cat: Size does not match.");
-		Image<float> rgbd(input.get_size_x(), input.get_size_y(), 4u);
-		for (size_t p = 0; p < (size_t)input.get_size_x() * input.get_size_y(); p++) {
-			for (int c = 0; c < 3; c++) rgbd.raw()[4 * p + c] = input.raw()[3 * p + c];
-			rgbd.raw()[4 * p + 3] = depth.raw()[p];
+			if (i + 1 >= argc) throw std::runtime_error(std::string("ERROR: option -") + o->name + " needs a value");
+			if (!values_.emplace(o->name, argv[i + 1]).second)
+				throw std::runtime_error(std::string("ERROR: option -") + o->name + " given twice");
+			i++;
 		}
-		input = rgbd;
+	}
+	std::string text(const char *name) const
+	{
+		auto it = values_.find(name);
+		if (it != values_.end()) return it->second;
+		for (const OptionSpec &o : kOptions)
+			if (strcmp(o.name, name) == 0) return o.default_value;
+		throw std::logic_error(std::string("no option ") + name);
+	}
+	int integer(const char *name) const { return atoi(text(name).c_str()); }
+	float real(const char *name) const { return (float)atof(text(name).c_str()); }
+	bool given(const char *name) const { return !text(name).empty(); }
+	const std::vector<std::string> &positional() const { return positional_; }
+	void usage(FILE *out) const
+	{
+		fprintf(out, "USAGE:\n%s input mask output [OPTIONS]\n\nAvailable options are:\n", program_.c_str());
+		for (const OptionSpec &o : kOptions) {
+			fprintf(out, o.help, text(o.name).c_str());
+			fputc('\n', out);
+		}
 	}
 
-	// automatic coarsest rate (Newson's rule, :160-177)
-	if (coarsest_rate == 0) coarsest_rate = std::min(1.5f * patch_side / max_hole_distance(mask), 1.f);
-	if (patch_side <= 0) throw std::runtime_error("ERROR: patch_side needs to be a positive integer.");
-	if ((coarsest_rate > 1) || (coarsest_rate < 0))
-		throw std::runtime_error("ERROR: coarsest rate should be between 0 and 1.");
-	if (inpainting_iterations < 0) throw std::runtime_error("ERROR: inpainting_iterations cannot be negative.");
-	if (confidence_decay_time <= 0.f) throw std::runtime_error("ERROR: confidence_decay_time needs to be positive.");
-	if ((lambda > 1.f) || (lambda < 0.f)) throw std::runtime_error("ERROR: lambda should be between 0 and 1.");
-	if (scales_amount < 1) throw std::runtime_error("ERROR: number of scales must be at least 1.");
-	if (std::abs(coarsest_rate - 1.0f) < 0.00001f) {
-		scales_amount = 1;
+  private:
+	std::string program_;
+	std::map<std::string, std::string> values_;
+	std::vector<std::string> positional_;
+};
+
+// ------------------------------------------------------------- settings
+// What a run needs, read from the command line and checked with the
+// reference's messages (main.cpp:160-215).
+struct Settings {
+	std::string input, mask, output;
+	std::string method, init_name;
+	std::string nnf_file, pyramid_prefix, depth_file;
+	int patch = 0, iterations = 0, scales = 0;
+	float coarse = 0, conf_decay = 0, conf_asym = 0, lambda = 0, psigma = 0, lambda_rgb = 0, lambda_d = 0;
+	ImageInpainting::InitType init = ImageInpainting::InitPoisson;
+	uint64_t seed = 0;
+};
+
+ImageInpainting::InitType init_type_named(const std::string &name)
+{
+	static const std::pair<const char *, ImageInpainting::InitType> kInits[] = {
+	    {"poisson", ImageInpainting::InitPoisson},
+	    {"black", ImageInpainting::InitBlack},
+	    {"avg", ImageInpainting::InitAvg},
+	    {"none", ImageInpainting::InitNone},
+	};
+	for (const auto &e : kInits)
+		if (name == e.first) return e.second;
+	throw std::runtime_error("ERROR: Unknown initialization type");
+}
+
+Settings read_settings(const CommandLine &cl)
+{
+	Settings s;
+	s.input = cl.positional()[0];
+	s.mask = cl.positional()[1];
+	s.output = cl.positional()[2];
+	s.method = cl.text("method");
+	s.init_name = cl.text("init");
+	s.nnf_file = cl.text("shownnf");
+	s.pyramid_prefix = cl.text("showpyr");
+	s.depth_file = cl.text("depth");
+	s.patch = cl.integer("patch");
+	s.iterations = cl.integer("iters");
+	s.scales = cl.integer("scales");
+	s.coarse = cl.real("coarse");
+	s.conf_decay = cl.real("conft");
+	s.conf_asym = cl.real("confa");
+	s.lambda = cl.real("lambda");
+	s.psigma = cl.real("psigma");
+	s.lambda_rgb = cl.real("lambdar");
+	s.lambda_d = cl.real("lambdad");
+	s.seed = cl.given("seed") ? strtoull(cl.text("seed").c_str(), nullptr, 10) : (uint64_t)time(NULL);
+	return s;
+}
+
+// The checks of main.cpp:178-215, after the automatic coarsest rate is known.
+void check_settings(Settings &s)
+{
+	if (s.patch <= 0) throw std::runtime_error("ERROR: patch_side needs to be a positive integer.");
+	if (s.coarse > 1 || s.coarse < 0) throw std::runtime_error("ERROR: coarsest rate should be between 0 and 1.");
+	if (s.iterations < 0) throw std::runtime_error("ERROR: inpainting_iterations cannot be negative.");
+	if (s.conf_decay <= 0.f) throw std::runtime_error("ERROR: confidence_decay_time needs to be positive.");
+	if (s.lambda > 1.f || s.lambda < 0.f) throw std::runtime_error("ERROR: lambda should be between 0 and 1.");
+	if (s.scales < 1) throw std::runtime_error("ERROR: number of scales must be at least 1.");
+	if (std::abs(s.coarse - 1.0f) < 0.00001f) {
+		s.scales = 1;
 		printf("\tnote: since the coarsest scale size ratio is 1.0, the number of scales is set to 1\n");
 	}
-	ImageInpainting::InitType init_type;
-	if (initialization_type_name == "poisson")
-		init_type = ImageInpainting::InitPoisson;
-	else if (initialization_type_name == "black")
-		init_type = ImageInpainting::InitBlack;
-	else if (initialization_type_name == "avg")
-		init_type = ImageInpainting::InitAvg;
-	else if (initialization_type_name == "none")
-		init_type = ImageInpainting::InitNone;
-	else
-		throw std::runtime_error("ERROR: Unknown initialization type");
+	s.init = init_type_named(s.init_name);
+}
 
-	const float tolerance = 0.1f;
-	const float subsampling_rate = ImageInpainting::calculate_subsampling_rate(coarsest_rate, scales_amount);
-	Shape patch(patch_side, patch_side);
-	const float weights_update_sigma = patch_sigma;
-	const int patch_match_iterations = 10, random_shots_limit = 30;
-	ImageInpainting image_inpainting(inpainting_iterations, tolerance, scales_amount, subsampling_rate,
-	                                 confidence_decay_time, confidence_asymptotic_value, init_type);
-	APatchDistance *patch_distance;
-	AImageUpdating *image_updating;
-	if (method_name == "nlmeans") {
-		image_updating = new PatchNonLocalMeans(patch, weights_update_sigma);
-		patch_distance = new L2NormPatchDistance(patch, weights_update_sigma);
-	} else if (method_name == "nlmedians") {
-		image_updating = new PatchNonLocalMedians(patch, weights_update_sigma);
-		patch_distance = new L1NormPatchDistance(patch, weights_update_sigma);
-	} else if (method_name == "nlpoisson") {
-		image_updating = new PatchNonLocalPoisson(patch, weights_update_sigma, lambda, 0.000001f, 1000);
-		patch_distance = new L2CombinedPatchDistance(lambda, patch, weights_update_sigma);
-	} else if (method_name == "nldepth") {
-		if (!depth_exists) throw std::runtime_error("Specify depth input using -depth [filename]");
-		image_updating = new PatchNonLocalDepth(patch, weights_update_sigma, lambda_rgb, lambda_d, 0.000001f, 1000);
-		patch_distance = new L2RGBDPatchDistance(lambda_rgb, lambda_d, patch, weights_update_sigma);
+// ---------------------------------------------------------------- inputs
+struct Inputs {
+	Image<float> image;  // L*a*b* (and depth as a fourth channel)
+	Mask mask;
+	bool has_depth = false;
+};
+
+Mask hole_mask(const Image<float> &m)
+{
+	Mask hole(m.get_size_x(), m.get_size_y());
+	bool any = false;
+	for (uint y = 0; y < m.get_size_y(); y++)
+		for (uint x = 0; x < m.get_size_x(); x++)
+			if (m.raw()[(size_t)y * m.get_size_x() + x] > 0) {
+				hole.mask(x, y);
+				any = true;
+			}
+	if (!any) throw std::runtime_error("ERROR: Mask should not be empty (all black)");
+	return hole;
+}
+
+Image<float> with_depth(const Image<float> &lab, const Image<float> &depth)
+{
+	if (depth.get_size_x() != lab.get_size_x() || depth.get_size_y() != lab.get_size_y())
+		throw std::runtime_error("cat: Size does not match.");
+	Image<float> rgbd(lab.get_size_x(), lab.get_size_y(), 4u);
+	const size_t n = (size_t)lab.get_size_x() * lab.get_size_y();
+	for (size_t p = 0; p < n; p++) {
+		std::copy(lab.raw() + 3 * p, lab.raw() + 3 * p + 3, rgbd.raw() + 4 * p);
+		rgbd.raw()[4 * p + 3] = depth.raw()[p];
+	}
+	return rgbd;
+}
+
+Inputs load_inputs(const Settings &s)
+{
+	Inputs in;
+	in.image = convert(rgb_image(read_image(s.input)), true);
+	const Image<float> m = mono_image(read_image(s.mask), s.mask);
+	if (in.image.get_size_x() != m.get_size_x() || in.image.get_size_y() != m.get_size_y())
+		throw std::runtime_error("ERROR: Input image and mask should be of the same size");
+	in.mask = hole_mask(m);
+	if (!s.depth_file.empty()) {
+		in.image = with_depth(in.image, mono_image(read_image(s.depth_file), s.depth_file));
+		in.has_depth = true;
+	}
+	return in;
+}
+
+// --------------------------------------------------------------- methods
+// A method: its image update and the patch distance the reference pairs it
+// with on the command line (main.cpp:245-263).  The inner CG solves run to
+// 1e-6 relative residual or 1000 iterations, as there.
+struct Method {
+	std::unique_ptr<APatchDistance> distance;
+	std::unique_ptr<AImageUpdating> updating;
+};
+
+Method make_method(const Settings &s, bool has_depth)
+{
+	Shape patch(s.patch, s.patch);  // the classes take it by non-const reference, as the reference's
+	Method m;
+	if (s.method == "nlmeans") {
+		m.updating.reset(new PatchNonLocalMeans(patch, s.psigma));
+		m.distance.reset(new L2NormPatchDistance(patch, s.psigma));
+	} else if (s.method == "nlmedians") {
+		m.updating.reset(new PatchNonLocalMedians(patch, s.psigma));
+		m.distance.reset(new L1NormPatchDistance(patch, s.psigma));
+	} else if (s.method == "nlpoisson") {
+		m.updating.reset(new PatchNonLocalPoisson(patch, s.psigma, s.lambda, 0.000001f, 1000));
+		m.distance.reset(new L2CombinedPatchDistance(s.lambda, patch, s.psigma));
+	} else if (s.method == "nldepth") {
+		if (!has_depth) throw std::runtime_error("Specify depth input using -depth [filename]");
+		m.updating.reset(new PatchNonLocalDepth(patch, s.psigma, s.lambda_rgb, s.lambda_d, 0.000001f, 1000));
+		m.distance.reset(new L2RGBDPatchDistance(s.lambda_rgb, s.lambda_d, patch, s.psigma));
 	} else {
 		throw std::runtime_error("ERROR: Unknown method name");
 	}
-	PatchMatch *patch_match = new PatchMatch(patch_distance, patch_match_iterations, random_shots_limit, -1);
-	image_inpainting.set_weights_updating(patch_match);
-	image_inpainting.set_image_updating(image_updating);
-	nli_dropin::set_seed(seed_opt[0] ? strtoull(seed_opt, nullptr, 10) : (uint64_t)time(NULL));
-	image_inpainting.keep_intermediate(!show_nnf_file.empty() || !show_pyramid_file.empty());
-	Image<float> output = image_inpainting.process(input, mask);
-	const nli_process_stats &st = image_inpainting.get_statistics();
+	return m;
+}
+
+// --------------------------------------------------------------- outputs
+// The result's file name, composed from the parameters as the reference
+// composes it (main.cpp:287-303), except that Poisson initialisation is
+// named "_initpoisson": the reference names it "_initnone" like -init none.
+std::string composed_name(const Settings &s)
+{
+	const char *init_tag = s.init == ImageInpainting::InitAvg     ? "_initavg"
+	                       : s.init == ImageInpainting::InitBlack ? "_init000"
+	                       : s.init == ImageInpainting::InitNone  ? "_initnone"
+	                                                               : "_initpoisson";
+	std::ostringstream o;
+	o << s.output << "_" << s.method;
+	if (s.method == "nlpoisson") o << "_l" << s.lambda;
+	o << "_sc" << s.scales << "_" << s.coarse << init_tag << "_ps" << s.patch << "_" << s.psigma << "_conf"
+	  << s.conf_decay << "_" << s.conf_asym << ".png";
+	return o.str();
+}
+
+void write_depth(const Image<float> &out)
+{
+	const int W = out.get_size_x(), H = out.get_size_y(), C = out.get_number_of_channels();
+	std::vector<float> d((size_t)W * H), grey3((size_t)W * H * 3);
+	for (size_t p = 0; p < d.size(); p++) {
+		d[p] = out.raw()[(size_t)C * p + 3];
+		std::fill(grey3.begin() + 3 * p, grey3.begin() + 3 * p + 3, d[p]);
+	}
+	write_image("inpainted_depth.pfm", d.data(), W, H, 1);
+	write_image("inpainted_depth.png", grey3.data(), W, H, 3);
+}
+
+void write_pyramid(const std::string &prefix, const std::vector<Image<float> > &levels)
+{
+	for (size_t n = 0; n < levels.size(); n++) {
+		const Image<float> rgb = convert(levels[n], false);
+		write_image(prefix + std::to_string(n) + ".png", rgb.raw(), rgb.get_size_x(), rgb.get_size_y(), 3);
+	}
+}
+
+// The illustration of the finest NNF (main.cpp:315-374): the result with the
+// hole boundary and every break of the field's offset between horizontal or
+// vertical neighbours in black.
+void write_nnf_illustration(const std::string &file, const Image<float> &rgb, const Mask &mask,
+                            const Image<Point> &nnf)
+{
+	const int W = rgb.get_size_x(), H = rgb.get_size_y();
+	std::vector<float> v(rgb.raw(), rgb.raw() + (size_t)W * H * 3);
+	auto offset = [&](int x, int y) {
+		const Point q = nnf((uint)x, (uint)y);
+		return std::make_pair(q.x - x, q.y - y);
+	};
+	for (int y = 1; y < H; y++)
+		for (int x = 1; x < W; x++) {
+			const bool inside = mask.test((uint)x, (uint)y);
+			bool dark = inside != mask.test((uint)x - 1, (uint)y) || inside != mask.test((uint)x, (uint)y - 1);
+			if (inside) dark = dark || offset(x - 1, y) != offset(x, y) || offset(x, y - 1) != offset(x, y);
+			if (dark) std::fill(v.begin() + 3 * ((size_t)y * W + x), v.begin() + 3 * ((size_t)y * W + x) + 3, 0.f);
+		}
+	write_image(file, v.data(), W, H, 3);
+}
+
+int run(int argc, char *argv[])
+{
+	const CommandLine cl(argc, argv);
+	if (cl.positional().size() < 3) {
+		cl.usage(stderr);
+		return 1;
+	}
+	Settings s = read_settings(cl);
+	const Inputs in = load_inputs(s);
+	// -coarse 0: the automatic coarsest rate (Newson's rule, main.cpp:160-177)
+	if (s.coarse == 0) s.coarse = std::min(1.5f * s.patch / max_hole_distance(in.mask), 1.f);
+	check_settings(s);
+
+	ImageInpainting inpainting(s.iterations, 0.1f, s.scales,
+	                           ImageInpainting::calculate_subsampling_rate(s.coarse, s.scales), s.conf_decay,
+	                           s.conf_asym, s.init);
+	Method method = make_method(s, in.has_depth);
+	PatchMatch weights(method.distance.get(), 10, 30, -1);
+	inpainting.set_weights_updating(&weights);
+	inpainting.set_image_updating(method.updating.get());
+	nli_dropin::set_seed(s.seed);
+	inpainting.keep_intermediate(!s.nnf_file.empty() || !s.pyramid_prefix.empty());
+	const Image<float> output = inpainting.process(in.image, in.mask);
+	const nli_process_stats &st = inpainting.get_statistics();
 	for (int i = st.scales - 1; i >= 0; i--)
 		printf("\tinpainting scale %d: %d iterations\n", st.scales - i, st.iterations[i]);
-	delete patch_match;
-	delete patch_distance;
-	delete image_updating;
 
-	std::stringstream output_str;
-	output_str << output_name << "_" << method_name;
-	if (method_name == "nlpoisson") output_str << "_l" << lambda;
-	output_str << "_sc" << scales_amount << "_" << coarsest_rate;
-	if (init_type == ImageInpainting::InitAvg)
-		output_str << "_initavg";
-	else if (init_type == ImageInpainting::InitBlack)
-		output_str << "_init000";
-	else
-		output_str << "_initnone";
-	output_str << "_ps" << patch_side << "_" << weights_update_sigma;
-	output_str << "_conf" << confidence_decay_time << "_" << confidence_asymptotic_value << ".png";
-	const int W = output.get_size_x(), H = output.get_size_y(), C = output.get_number_of_channels();
-	Image<float> rgb = convert(output, false);
-	write_image(output_str.str(), rgb.raw(), W, H, 3);
-	printf("%s\n", output_str.str().c_str());
-	if (depth_exists) {
-		std::vector<float> d((size_t)W * H), d3((size_t)W * H * 3);
-		for (size_t p = 0; p < d.size(); p++) d[p] = d3[3 * p] = d3[3 * p + 1] = d3[3 * p + 2] = output.raw()[(size_t)C * p + 3];
-		write_image("inpainted_depth.pfm", d.data(), W, H, 1);
-		write_image("inpainted_depth.png", d3.data(), W, H, 3);
-	}
-	if (!show_pyramid_file.empty()) {
-		std::vector<Image<float> > pyr = image_inpainting.get_output_image_pyramid();
-		for (size_t n = 0; n < pyr.size(); n++) {
-			std::stringstream s;
-			s << show_pyramid_file << n << ".png";
-			Image<float> lv = convert(pyr[n], false);
-			write_image(s.str(), lv.raw(), lv.get_size_x(), lv.get_size_y(), 3);
-		}
-	}
-	// NNF illustration: hole boundary and NNF discontinuities in black (:320-372)
-	if (!show_nnf_file.empty()) {
-		std::vector<Image<Point> > nnf_pyramid = image_inpainting.get_nnf_pyramid();
-		Image<Point> last = nnf_pyramid[nnf_pyramid.size() - 1];
-		Image<float> show = rgb;
-		float *sv = show.raw();
-		for (int c = 0; c < 3; c++)
-			for (int y = 1; y < H; y++)
-				for (int x = 1; x < W; x++) {
-					const bool m = mask.test((uint)x, (uint)y);
-					if (m != mask.test((uint)x - 1, (uint)y) || m != mask.test((uint)x, (uint)y - 1))
-						sv[((size_t)y * W + x) * 3 + c] = 0;
-					if (m) {
-						const Point a = last((uint)x - 1, (uint)y), b = last((uint)x, (uint)y);
-						if (a.x - (x - 1) != b.x - x || a.y - y != b.y - y) sv[((size_t)y * W + x) * 3 + c] = 0;
-						const Point u = last((uint)x, (uint)y - 1);
-						if (u.x - x != b.x - x || u.y - (y - 1) != b.y - y) sv[((size_t)y * W + x) * 3 + c] = 0;
-					}
-				}
-		write_image(show_nnf_file, sv, W, H, 3);
-	}
+	const std::string name = composed_name(s);
+	const Image<float> rgb = convert(output, false);
+	write_image(name, rgb.raw(), rgb.get_size_x(), rgb.get_size_y(), 3);
+	printf("%s\n", name.c_str());
+	if (in.has_depth) write_depth(output);
+	if (!s.pyramid_prefix.empty()) write_pyramid(s.pyramid_prefix, inpainting.get_output_image_pyramid());
+	if (!s.nnf_file.empty()) write_nnf_illustration(s.nnf_file, rgb, in.mask, inpainting.get_nnf_pyramid().back());
 	return 0;
 }
 

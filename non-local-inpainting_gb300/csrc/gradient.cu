@@ -9,15 +9,7 @@ namespace nli {
 // pixel and channel; consecutive threads touch consecutive addresses.
 __global__ void k_gradient(const float *__restrict__ img, int W, int H, int C, float *__restrict__ grad)
 {
-	const int n = W * H * C;
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		const int p = i / C;
-		const int x = p % W, y = p / W;
-		const float v = img[i];
-		const float gx = (x == W - 1) ? 0.0f : __fsub_rn(img[i + C], v);
-		const float gy = (y == H - 1) ? 0.0f : __fsub_rn(img[i + (size_t)C * W], v);
-		reinterpret_cast<float2 *>(grad)[i] = make_float2(gx, gy);
-	}
+	gradient_span(img, W, H, C, grad, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 void launch_gradient(cudaStream_t s, const float *img, int W, int H, int C, float *grad)
@@ -33,16 +25,7 @@ void launch_gradient(cudaStream_t s, const float *img, int W, int H, int C, floa
 // repeating the last ones so that forward differences there are exactly 0.
 __global__ void k_pad4(const float *__restrict__ img, int W, int H, int C, float4 *__restrict__ out)
 {
-	const int Wp = W + 1, n = Wp * (H + 1);
-	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-		const int y = i / Wp, x = i - y * Wp;
-		const float *u = img + ((size_t)min(y, H - 1) * W + min(x, W - 1)) * C;
-		float4 v = make_float4(u[0], 0.f, 0.f, 0.f);
-		if (C > 1) v.y = u[1];
-		if (C > 2) v.z = u[2];
-		if (C > 3) v.w = u[3];
-		out[i] = v;
-	}
+	pad4_span(img, W, H, C, out, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 void launch_pad4(cudaStream_t s, const float *img, int W, int H, int C, float4 *out)

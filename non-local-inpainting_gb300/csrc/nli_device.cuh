@@ -10,6 +10,51 @@
 namespace nli {
 
 // ------------------------------------------------------------------------
+// Checked builds (NLI_CHECKED).  Data-dependent gathered indices (PatchMatch
+// candidate windows, NNF-shifted pixels, hole lists, CG neighbour codes) go
+// through nli_in_bounds: in a checked build an index outside [0, n) is
+// recorded -- the first one per translation unit, as (site << 32) | index --
+// and the access is skipped; otherwise the test compiles away.  The record
+// is read and cleared by nli_debug_check_status.
+enum CheckSite : unsigned {
+	kSitePmSource = 1,    // PatchMatch: source window row of a candidate
+	kSitePmMask = 2,      // PatchMatch: source mask at a candidate
+	kSitePmField = 3,     // PatchMatch: a neighbour's match / the initial field
+	kSitePmTarget = 4,    // PatchMatch: target list entry
+	kSiteMeansSource = 10,  // NL-means / NL-medians: NNF-shifted source pixel
+	kSiteHole = 11,         // hole list entry
+	kSiteCoefSource = 12,   // NL-Poisson coefficient gather: NNF-shifted pixel
+	kSiteCgNeighbour = 13,  // CG: neighbour code (owning CTA, index)
+	kSiteScaleNnf = 20,     // scale transition: scaled field position
+};
+
+#ifdef NLI_CHECKED
+static __device__ unsigned long long g_nli_check_word;
+
+__device__ __forceinline__ bool nli_in_bounds(long long i, long long n, unsigned site)
+{
+	if (i >= 0 && i < n) return true;
+	atomicCAS(&g_nli_check_word, 0ull, ((unsigned long long)site << 32) | (unsigned long long)(unsigned)i);
+	return false;
+}
+
+// Host reader of this translation unit's record (read and cleared).
+#define NLI_CHECK_READER(fn)                                                           \
+	unsigned long long fn()                                                            \
+	{                                                                                  \
+		unsigned long long v = 0, z = 0;                                               \
+		NLI_CUDA(cudaMemcpyFromSymbol(&v, g_nli_check_word, sizeof(v)));              \
+		NLI_CUDA(cudaMemcpyToSymbol(g_nli_check_word, &z, sizeof(z)));                \
+		return v;                                                                      \
+	}
+#else
+__device__ __forceinline__ bool nli_in_bounds(long long, long long, unsigned) { return true; }
+
+#define NLI_CHECK_READER(fn) \
+	unsigned long long fn() { return 0; }
+#endif
+
+// ------------------------------------------------------------------------
 // Reference-exact arithmetic.  The reference is compiled for the host with
 // separate IEEE roundings for every product and sum (no fused multiply-add);
 // these wrappers keep the CUDA compiler from contracting them.
@@ -167,6 +212,41 @@ __device__ inline float dist_exact(const DistArgs &a, const float *__restrict__ 
 }
 
 // ------------------------------------------------------------------------
+// Forward differences (k_gradient): elements first, first + stride, ... of
+// the W * H * C values; output 2C interleaved channels per pixel.
+__device__ __forceinline__ void gradient_span(const float *__restrict__ img, int W, int H, int C,
+                                              float *__restrict__ grad, int first, int stride)
+{
+	const int n = W * H * C;
+	for (int i = first; i < n; i += stride) {
+		const int p = i / C;
+		const int x = p % W, y = p / W;
+		const float v = img[i];
+		const float gx = (x == W - 1) ? 0.0f : __fsub_rn(img[i + C], v);
+		const float gy = (y == H - 1) ? 0.0f : __fsub_rn(img[i + (size_t)C * W], v);
+		reinterpret_cast<float2 *>(grad)[i] = make_float2(gx, gy);
+	}
+}
+
+// ------------------------------------------------------------------------
+// Padded float4 pixels (k_pad4): elements first, first + stride, ... of the
+// (W + 1) x (H + 1) grid, the extra column and row repeating the last ones.
+__device__ __forceinline__ void pad4_span(const float *__restrict__ img, int W, int H, int C, float4 *__restrict__ out,
+                                          int first, int stride)
+{
+	const int Wp = W + 1, n = Wp * (H + 1);
+	for (int i = first; i < n; i += stride) {
+		const int y = i / Wp, x = i - y * Wp;
+		const float *u = img + ((size_t)min(y, H - 1) * W + min(x, W - 1)) * C;
+		float4 v = make_float4(u[0], 0.f, 0.f, 0.f);
+		if (C > 1) v.y = u[1];
+		if (C > 2) v.z = u[2];
+		if (C > 3) v.w = u[3];
+		out[i] = v;
+	}
+}
+
+// ------------------------------------------------------------------------
 // Reductions.
 __device__ __forceinline__ double warp_sum(double v)
 {
@@ -201,13 +281,16 @@ __device__ __forceinline__ double block_sum(double v, double *smem /* BLOCK/32 *
 
 // ------------------------------------------------------------------------
 // Grid-wide barrier for cooperatively launched kernels (all blocks are
-// co-resident).  Spins at most `limit` polls; on expiry it records a
-// timeout in the status block and returns false so the kernel can leave.
-__device__ __forceinline__ bool grid_barrier(DevStatus *st, unsigned nblocks, unsigned limit = 1u << 26)
+// co-resident).  Spins at most st->wait_limit polls (2^26 when 0); on
+// expiry it records a timeout in the status block and returns false so the
+// kernel can leave.
+__device__ __forceinline__ bool grid_barrier(DevStatus *st, unsigned nblocks)
 {
 	__syncthreads();
 	bool ok = true;
 	if (threadIdx.x == 0) {
+		const unsigned set = *(volatile unsigned *)&st->wait_limit;
+		const unsigned limit = set ? set : (1u << 26);
 		volatile unsigned *gen = &st->barrier_gen;
 		unsigned g = *gen;
 		__threadfence();

@@ -83,7 +83,7 @@ struct DevStatus {
 	unsigned int barrier_count;
 	unsigned int barrier_gen;
 	int timeout;
-	int pad;
+	unsigned int wait_limit;  // grid barrier polls before giving up (0: the default)
 	unsigned long long pm_calls;
 };
 
@@ -132,6 +132,8 @@ struct nli_ctx {
 	int tune_cg_precond = 0;             // NL-Poisson CG: 0 plain (the reference's), 1 Jacobi
 	int tune_graph_loop = 1;             // iterations 1.. of a scale as one CUDA graph (while node):
 	                                     // 1 in nli_process only, 2 also in batches, 0 never
+	int tune_cg_single_max = 1024;       // CG systems of at most this many unknowns: one CTA
+	int tune_batch_mode = 1;             // batches: 1 lockstep (lockstep.cu), 0 worker contexts (batch.cu)
 	bool batch_worker = false;           // a worker context of nli_process_batch
 	int max_smem_optin = 0;              // dynamic shared memory per block at most
 	std::vector<nli_ctx *> workers;
@@ -261,6 +263,30 @@ void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patch
                     int32_t *out_nnf, float *out_dist, double *energy, const int32_t *tlist = nullptr,
                     int n_target = -1, PatchMatchMetricsHost *metrics = nullptr);
 
+// Batched PatchMatch (lockstep batch driver): one image's call.  The image
+// is both source and target; the driver supplies the scratch buffers.
+constexpr int kBatchMax = 64;  // images per batched launch
+struct PmBatchItem {
+	const float *img;
+	int W, H;
+	const uint8_t *smask, *tmask;
+	const int32_t *tlist;
+	int nt;
+	const int32_t *init;  // initial field or null
+	int32_t *out;         // result field, W * H int2
+	float4 *pad;          // (W + 1) * (H + 1) padded pixels
+	int32_t *nnf_y;       // W * H int2
+	float *dist_x, *dist_y;  // W * H
+	uint64_t seed;
+	unsigned long long *calls;    // the image's PatchMatch call index (device)
+	unsigned long long *counter;  // the image's candidate counters (2, device) or null
+	int flag;                     // index of the image's active flag
+};
+// active: device flags (null: all), item i reads active[items[i].flag];
+// inactive images are skipped.
+void patchmatch_batch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patchmatch_params &pm, int C, int n,
+                          const PmBatchItem *items, const int *active);
+
 // update.cu
 // read_back false: nothing is read to the host; *total_dev (if given)
 // receives the device address of the step's sum (du)^2 and *cg_iters_dev
@@ -269,6 +295,27 @@ double update_run(nli_ctx *ctx, const nli_update_params &up, float *image, const
                   const uint8_t *dom, const uint8_t *ext, const int32_t *nnf, const float *conf, int W,
                   int H, int C, const int32_t *hole_list = nullptr, int n_hole = -1,
                   bool read_back = true, const double **total_dev = nullptr, const int **cg_iters_dev = nullptr);
+
+// Batched update (lockstep batch driver): one image's step.  The image is
+// updated in place on its hole; orig as in update_run.
+struct UpdBatchItem {
+	int W, H;
+	float *img;
+	const float *orig;
+	const uint8_t *dom, *ext;
+	const int32_t *nnf;
+	const float *conf;
+	const int32_t *hole;
+	int nh;
+	double *total;  // device: the step's sum of (du)^2
+	int *cg_iters;  // device: CG iterations per channel (4 ints; NL-Poisson / NL-depth)
+	int flag;       // index of the image's active flag
+};
+// ups[i]: image i's update parameters (the patch and sigma are shared);
+// active: device flags (null: all), item i reads active[items[i].flag].  Scratch lives in the
+// context's workspace under per-image names; a first call sizes it.
+void update_batch_run(nli_ctx *ctx, const nli_update_params *ups, int C, int n, const UpdBatchItem *items,
+                      const int *active);
 
 // Adjoint of one update with the NNF fixed (update.cu).
 void update_backward_run(nli_ctx *ctx, const nli_update_params &up, const float *image, const float *out,
@@ -298,6 +345,18 @@ void process_batch_run(nli_ctx *ctx, int n, const nli_process_params *params, co
                        const uint8_t *const *masks, const int32_t *widths, const int32_t *heights,
                        const int32_t *channels, float *const *outputs, nli_process_stats *stats, int32_t *status,
                        bool host_buffers);
+
+// process.cu: the lockstep form of process_batch_run (NLI_TUNE_BATCH_MODE 1)
+void lockstep_batch_run(nli_ctx *ctx, int n, const nli_process_params *params, const float *const *images,
+                        const uint8_t *const *masks, const int32_t *widths, const int32_t *heights,
+                        const int32_t *channels, float *const *outputs, nli_process_stats *stats, int32_t *status,
+                        bool host_buffers);
+
+// Records of the checked build's bounds tests, one per translation unit
+// with instrumented kernels (0 elsewhere; read and cleared).
+unsigned long long check_word_patchmatch();
+unsigned long long check_word_update();
+unsigned long long check_word_process();
 
 // color.cu
 void rgb_to_lab_run(nli_ctx *ctx, const float *rgb, int n, float *lab);

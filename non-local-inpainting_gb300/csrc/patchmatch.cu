@@ -159,7 +159,8 @@ struct Kind {
 // latter through their margin; user masks may not).
 __device__ __forceinline__ bool src_ok(const PmArgs &p, int x, int y)
 {
-	return x >= p.rx && y >= p.ry && x + p.ex <= p.sW && y + p.ey <= p.sH && p.smask[y * p.sW + x];
+	return x >= p.rx && y >= p.ry && x + p.ex <= p.sW && y + p.ey <= p.sH &&
+	       nli_in_bounds((long long)y * p.sW + x, (long long)p.sW * p.sH, kSitePmMask) && p.smask[y * p.sW + x];
 }
 
 __device__ __forceinline__ bool tgt_patch_inside(const PmArgs &p, int x, int y)
@@ -379,6 +380,14 @@ __device__ __forceinline__ void eval_candidates(const PmArgs &p, const float *s_
 		const int cand = __shfl_sync(kFull, mycand, active ? idx : 0);
 		const int cx = cand & 0xffff, cy = cand >> 16;
 		const float4 *S = p.src + (size_t)(cy - p.ry) * sWp + (cx - p.rx) + c;
+		// row r of this lane's column of the candidate's window (a checked
+		// build tests the index against the padded source)
+		const long long s_base = (long long)(cy - p.ry) * (long long)sWp + (cx - p.rx) + c;
+		const long long s_n = (long long)sWp * (p.sH + 1);
+		auto ldrow = [&](int r) -> float4 {
+			return nli_in_bounds(s_base + (long long)r * (long long)sWp, s_n, kSitePmSource) ? __ldg(S + (size_t)r * sWp)
+			                                                                                 : zero;
+		};
 		const float4 *T = s_t + c;
 		const float *Wt = s_w + c;
 		const float4 *Sl = nullptr;  // this lane's column of its candidate's staged window
@@ -411,8 +420,8 @@ __device__ __forceinline__ void eval_candidates(const PmArgs &p, const float *s_
 			ts->phase ^= 1u;
 			Sl = ts->slots + (active ? sw : 0) * ts->slot_stride + c;
 		}
-		float4 v0 = (!TMA && active) ? __ldg(S) : zero;
-		float4 v1 = (!TMA && PF == 2 && active && rows > 1) ? __ldg(S + sWp) : zero;
+		float4 v0 = (!TMA && active) ? ldrow(0) : zero;
+		float4 v1 = (!TMA && PF == 2 && active && rows > 1) ? ldrow(1) : zero;
 		float4 dp = zero;
 		float wp = 0.f;
 		Acc A = {0.f, 0.f, 0.f, 0.f};
@@ -424,9 +433,9 @@ __device__ __forceinline__ void eval_candidates(const PmArgs &p, const float *s_
 				v = active ? Sl[r * L] : zero;
 			} else if (PF == 2) {
 				v0 = v1;
-				v1 = (active && r + 2 < rows) ? __ldg(S + (size_t)(r + 2) * sWp) : zero;
+				v1 = (active && r + 2 < rows) ? ldrow(r + 2) : zero;
 			} else {
-				v0 = (active && r + 1 < rows) ? __ldg(S + (size_t)(r + 1) * sWp) : zero;
+				v0 = (active && r + 1 < rows) ? ldrow(r + 1) : zero;
 			}
 			float4 t;
 			if constexpr (V == kPmRegs)
@@ -561,6 +570,53 @@ __device__ __forceinline__ PmSmem pm_smem(const DistArgs &a, const PmArgs &p)
 	return m;
 }
 
+// One target point of the initial field (patch_match.cpp:329-381): its
+// seed match (the init field's, else random draws), and that match's
+// distance.  Called by one whole warp; lane 0 writes the results.
+template <int KIND, int C, int P, int V>
+__device__ __forceinline__ void pm_init_point(const PmArgs &p, const PmSmem &m, TmaState &ts, float4 *tw,
+                                              const uint2 key, int pix, const int2 *__restrict__ init,
+                                              int2 *__restrict__ nnf, float *__restrict__ dist, unsigned &evals,
+                                              unsigned &partial)
+{
+	const int lane = threadIdx.x & 31;
+	if (!nli_in_bounds(pix, (long long)p.tW * p.tH, kSitePmTarget)) return;
+	const int x = pix % p.tW, y = pix / p.tW;
+	Rng rng(key, (uint32_t)pix, 0xffffffffu);
+	int2 n = init ? init[pix] : make_int2(-1, -1);
+	int tries = 0;
+	// patch_match.cpp:341-381: keep a seed match that lies in the
+	// source, otherwise redraw it uniformly up to `shots` times
+	if (init) {
+		while (!src_ok(p, n.x, n.y) && tries < p.shots) {
+			n.x = rng.below(p.sW);
+			n.y = rng.below(p.sH);
+			tries++;
+		}
+	} else {
+		while ((n.x < 0 || !src_ok(p, n.x, n.y)) && tries < p.shots) {
+			n.x = rng.below(p.sW);
+			n.y = rng.below(p.sH);
+			tries++;
+		}
+	}
+	float d = FLT_MAX;
+	int2 best = make_int2(-1, -1);
+	if (src_ok(p, n.x, n.y) && tgt_patch_inside(p, x, y)) {
+		if constexpr (V == kPmRegs)
+			load_window_regs<KIND, C, P>(p, m.w, x, y, tw);
+		else
+			load_window<C>(p, m.w, x, y, m.t);
+		eval_candidates<KIND, C, P, V>(p, m.w, m.t, n.x | (n.y << 16), 1, best, d, partial, &ts, tw);
+		evals++;
+		__syncwarp();
+	}
+	if (lane == 0) {
+		nnf[pix] = best;
+		dist[pix] = d;
+	}
+}
+
 template <int KIND, int C, int P, int V>
 __global__ void __launch_bounds__(pm_threads(V), 1) k_pm_init(DistArgs a, PmArgs p, const int2 *__restrict__ init,
                                                       int2 *__restrict__ nnf, float *__restrict__ dist,
@@ -581,46 +637,93 @@ __global__ void __launch_bounds__(pm_threads(V), 1) k_pm_init(DistArgs a, PmArgs
 	// neighbourhoods in L1
 	const int chunk = (p.nt + gridDim.x - 1) / gridDim.x;
 	const int end = min(p.nt, (int)(blockIdx.x + 1) * chunk);
-	for (int wi = blockIdx.x * chunk + (threadIdx.x >> 5); wi < end; wi += blockDim.x >> 5) {
-		const int pix = p.tlist[wi];
-		const int x = pix % p.tW, y = pix / p.tW;
-		Rng rng(key, (uint32_t)pix, 0xffffffffu);
-		int2 n = init ? init[pix] : make_int2(-1, -1);
-		int tries = 0;
-		// patch_match.cpp:341-381: keep a seed match that lies in the
-		// source, otherwise redraw it uniformly up to `shots` times
-		if (init) {
-			while (!src_ok(p, n.x, n.y) && tries < p.shots) {
-				n.x = rng.below(p.sW);
-				n.y = rng.below(p.sH);
-				tries++;
-			}
-		} else {
-			while ((n.x < 0 || !src_ok(p, n.x, n.y)) && tries < p.shots) {
-				n.x = rng.below(p.sW);
-				n.y = rng.below(p.sH);
-				tries++;
-			}
-		}
-		float d = FLT_MAX;
-		int2 best = make_int2(-1, -1);
-		if (src_ok(p, n.x, n.y) && tgt_patch_inside(p, x, y)) {
-			if constexpr (V == kPmRegs)
-				load_window_regs<KIND, C, P>(p, m.w, x, y, tw);
-			else
-				load_window<C>(p, m.w, x, y, m.t);
-			eval_candidates<KIND, C, P, V>(p, m.w, m.t, n.x | (n.y << 16), 1, best, d, partial, &ts, tw);
-			evals++;
-			__syncwarp();
-		}
-		if (lane == 0) {
-			nnf[pix] = best;
-			dist[pix] = d;
-		}
-	}
+	for (int wi = blockIdx.x * chunk + (threadIdx.x >> 5); wi < end; wi += blockDim.x >> 5)
+		pm_init_point<KIND, C, P, V>(p, m, ts, tw, key, p.tlist[wi], init, nnf, dist, evals, partial);
 	if (lane == 0 && evals) {
 		atomicAdd(counter, (unsigned long long)evals);
 		if (partial) atomicAdd(counter + 1, (unsigned long long)partial);
+	}
+}
+
+// metric_prop (may be NULL): this sweep's count of target points that the
+// propagation step improved; metric_shots (may be NULL): the largest index
+// of a first accepted random draw (patch_match.cpp:452-456, 481-485).
+// One target point of a sweep: propagation from the previous sweep's
+// field, then random search around the best match.  Called by one whole
+// warp; lane 0 writes the results.
+template <int KIND, int C, int P, int V>
+__device__ __forceinline__ void pm_sweep_point(const PmArgs &p, const PmSmem &m, TmaState &ts, float4 *tw,
+                                               const uint2 key, int windows, int pix, int sweep, int jump,
+                                               const int2 *__restrict__ nnf_in, const float *__restrict__ dist_in,
+                                               int2 *__restrict__ nnf_out, float *__restrict__ dist_out,
+                                               unsigned &evals, unsigned &partial, unsigned &improved, int &max_shot)
+{
+	const int lane = threadIdx.x & 31;
+	if (!nli_in_bounds(pix, (long long)p.tW * p.tH, kSitePmTarget)) return;
+	const int x = pix % p.tW, y = pix / p.tW;
+	int2 best = nnf_in[pix];
+	float bd = dist_in[pix];
+	if (tgt_patch_inside(p, x, y)) {
+		if constexpr (V == kPmRegs)
+			load_window_regs<KIND, C, P>(p, m.w, x, y, tw);
+		else
+			load_window<C>(p, m.w, x, y, m.t);
+		// propagation: lane 4s + k proposes the match of neighbour k
+		// (left, right, up, down) at distance 1 (s = 0) or at the jump
+		// distance (s = 1), shifted back by the neighbour's offset
+		bool valid = false;
+		int packed = 0;
+		if (lane < (jump > 1 ? 8 : 4)) {
+			const int s = (lane < 4) ? 1 : jump, k = lane & 3;
+			const int nx = x + ((k == 0) ? -s : (k == 1) ? s : 0);
+			const int ny = y + ((k == 2) ? -s : (k == 3) ? s : 0);
+			if (tgt_ok(p, nx, ny) && nli_in_bounds((long long)ny * p.tW + nx, (long long)p.tW * p.tH, kSitePmField)) {
+				const int2 q = nnf_in[ny * p.tW + nx];
+				if (q.x >= 0) {
+					const int cx = q.x + (x - nx), cy = q.y + (y - ny);
+					valid = src_ok(p, cx, cy);
+					packed = cx | (cy << 16);
+				}
+			}
+		}
+		int mycand;
+		int n = compact_candidates(valid, packed, best, m.list, mycand);
+		evals += n;
+		const float bd_before = bd;
+		eval_candidates<KIND, C, P, V>(p, m.w, m.t, mycand, n, best, bd, partial, &ts, tw);
+		if (bd < bd_before) improved++;
+		// random search around the match after propagation: lane k draws
+		// in window max_window >> k from its own stream, up to `shots`
+		// draws, and proposes the first that lands in the source
+		valid = false;
+		if (lane < windows) {
+			const int w = p.max_window >> lane;
+			const int x_min = max(best.x - w, 0), y_min = max(best.y - w, 0);
+			const int x_max = min(best.x + w + 1, p.sW), y_max = min(best.y + w + 1, p.sH);
+			Rng rng(key, (uint32_t)pix, (uint32_t)sweep, (uint32_t)lane);
+#pragma unroll 1
+			for (int t = 0; t < p.shots; t++) {
+				const int rx = x_min + rng.below(x_max - x_min);
+				const int ry = y_min + rng.below(y_max - y_min);
+				if (src_ok(p, rx, ry)) {
+					valid = true;
+					packed = rx | (ry << 16);
+					max_shot = max(max_shot, t);
+					break;
+				}
+			}
+		}
+		n = compact_candidates(valid, packed, best, m.list, mycand);
+		evals += n;
+		eval_candidates<KIND, C, P, V>(p, m.w, m.t, mycand, n, best, bd, partial, &ts, tw);
+		__syncwarp();
+	} else {
+		best = make_int2(-1, -1);
+		bd = FLT_MAX;
+	}
+	if (lane == 0) {
+		nnf_out[pix] = best;
+		dist_out[pix] = bd;
 	}
 }
 
@@ -648,74 +751,9 @@ __global__ void __launch_bounds__(pm_threads(V), 1) k_pm_sweep(DistArgs a, PmArg
 	const int windows = 32 - __clz(p.max_window);
 	const int chunk = (p.nt + gridDim.x - 1) / gridDim.x;
 	const int end = min(p.nt, (int)(blockIdx.x + 1) * chunk);
-	for (int wi = blockIdx.x * chunk + (threadIdx.x >> 5); wi < end; wi += blockDim.x >> 5) {
-		const int pix = p.tlist[wi];
-		const int x = pix % p.tW, y = pix / p.tW;
-		int2 best = nnf_in[pix];
-		float bd = dist_in[pix];
-		if (tgt_patch_inside(p, x, y)) {
-			if constexpr (V == kPmRegs)
-				load_window_regs<KIND, C, P>(p, m.w, x, y, tw);
-			else
-				load_window<C>(p, m.w, x, y, m.t);
-			// propagation: lane 4s + k proposes the match of neighbour k
-			// (left, right, up, down) at distance 1 (s = 0) or at the jump
-			// distance (s = 1), shifted back by the neighbour's offset
-			bool valid = false;
-			int packed = 0;
-			if (lane < (jump > 1 ? 8 : 4)) {
-				const int s = (lane < 4) ? 1 : jump, k = lane & 3;
-				const int nx = x + ((k == 0) ? -s : (k == 1) ? s : 0);
-				const int ny = y + ((k == 2) ? -s : (k == 3) ? s : 0);
-				if (tgt_ok(p, nx, ny)) {
-					const int2 q = nnf_in[ny * p.tW + nx];
-					if (q.x >= 0) {
-						const int cx = q.x + (x - nx), cy = q.y + (y - ny);
-						valid = src_ok(p, cx, cy);
-						packed = cx | (cy << 16);
-					}
-				}
-			}
-			int mycand;
-			int n = compact_candidates(valid, packed, best, m.list, mycand);
-			evals += n;
-			const float bd_before = bd;
-			eval_candidates<KIND, C, P, V>(p, m.w, m.t, mycand, n, best, bd, partial, &ts, tw);
-			if (bd < bd_before) improved++;
-			// random search around the match after propagation: lane k draws
-			// in window max_window >> k from its own stream, up to `shots`
-			// draws, and proposes the first that lands in the source
-			valid = false;
-			if (lane < windows) {
-				const int w = p.max_window >> lane;
-				const int x_min = max(best.x - w, 0), y_min = max(best.y - w, 0);
-				const int x_max = min(best.x + w + 1, p.sW), y_max = min(best.y + w + 1, p.sH);
-				Rng rng(key, (uint32_t)pix, (uint32_t)sweep, (uint32_t)lane);
-#pragma unroll 1
-				for (int t = 0; t < p.shots; t++) {
-					const int rx = x_min + rng.below(x_max - x_min);
-					const int ry = y_min + rng.below(y_max - y_min);
-					if (src_ok(p, rx, ry)) {
-						valid = true;
-						packed = rx | (ry << 16);
-						max_shot = max(max_shot, t);
-						break;
-					}
-				}
-			}
-			n = compact_candidates(valid, packed, best, m.list, mycand);
-			evals += n;
-			eval_candidates<KIND, C, P, V>(p, m.w, m.t, mycand, n, best, bd, partial, &ts, tw);
-			__syncwarp();
-		} else {
-			best = make_int2(-1, -1);
-			bd = FLT_MAX;
-		}
-		if (lane == 0) {
-			nnf_out[pix] = best;
-			dist_out[pix] = bd;
-		}
-	}
+	for (int wi = blockIdx.x * chunk + (threadIdx.x >> 5); wi < end; wi += blockDim.x >> 5)
+		pm_sweep_point<KIND, C, P, V>(p, m, ts, tw, key, windows, p.tlist[wi], sweep, jump, nnf_in, dist_in, nnf_out,
+		                              dist_out, evals, partial, improved, max_shot);
 	if (lane == 0 && evals) {
 		atomicAdd(counter, (unsigned long long)evals);
 		if (partial) atomicAdd(counter + 1, (unsigned long long)partial);
@@ -763,10 +801,9 @@ __global__ void k_energy(const int32_t *__restrict__ tlist, int nt, const float 
 
 // Jump distance of a sweep: 16, 8, 4, 2, 16, 8, ... (never above half the
 // larger target side).
-static int jump_for(int sweep, int tW, int tH)
+__host__ __device__ inline int jump_for(int sweep, int tW, int tH)
 {
-	static const int seq[4] = {16, 8, 4, 2};
-	int j = seq[sweep % 4];
+	int j = 16 >> (sweep % 4);
 	while (j > 1 && 2 * j > max(tW, tH)) j /= 2;
 	return j;
 }
@@ -897,6 +934,312 @@ static void sweep_energy(cudaStream_t s, const PmArgs &p, const float *dist, con
 	NLI_CHECK_LAUNCH();
 	launch_sum_partials(s, m.partials, m.partial_blocks, m.energy + sweep);
 }
+
+// ====================================================== batched launches
+// PatchMatch calls of up to kBatchMax images in one launch per kernel (the
+// lockstep batch driver, lockstep.cu).  Every image is both source and
+// target (as in the inpainting driver), with its own sizes, masks, target
+// list, seed and call index; the distance, patch and PatchMatch parameters
+// are shared.  Per target point the work is exactly that of the one-image
+// kernels (the same device functions, Philox streams keyed by the image's
+// own seed and call index), so each image's field equals its one-image
+// call's bit for bit.
+//
+// The per-image arguments travel in the kernel's parameter space (a
+// __grid_constant__ table read through the constant cache, not the L1 data
+// pipe that bounds the sweep).  The persistent kernels see the concatenated
+// target lists of the images still iterating (their `active` flag, written
+// on the device between iterations) as one work list: block b takes the
+// contiguous range [b * chunk, (b + 1) * chunk) of it, its warps interleaved
+// over the range, so an image's points stay together in L1 as in the
+// one-image kernels.
+struct PmBatchTask {
+	PmArgs p;
+	int flag;            // index of the image's active flag
+	unsigned long long *counter;  // the image's candidate counters (2)
+	const float *img;    // the image (source = target), HWC float
+	const int2 *init;    // initial field or null
+	int2 *nnf_x, *nnf_y;  // result (x) and the sweeps' second buffer
+	float *dist_x, *dist_y;
+};
+
+struct PmBatchArgs {
+	int n;
+	const int *active;  // per image: still iterating (null: all)
+	PmBatchTask t[kBatchMax];
+};
+
+__device__ __forceinline__ bool batch_on(const int *active, int t) { return !active || active[t] != 0; }
+
+// Exclusive prefix of the active images' target counts in s_pre[0..n]
+// (s_pre[n] is the total); the whole block calls it.
+__device__ __forceinline__ int pm_batch_prefix(const PmBatchArgs &B, int *s_pre)
+{
+	if (threadIdx.x < 32) {
+		const int lane = threadIdx.x;
+		const int t0 = 2 * lane, t1 = t0 + 1;
+		const int v0 = (t0 < B.n && batch_on(B.active, B.t[t0].flag)) ? B.t[t0].p.nt : 0;
+		const int v1 = (t1 < B.n && batch_on(B.active, B.t[t1].flag)) ? B.t[t1].p.nt : 0;
+		int incl = v0 + v1;
+#pragma unroll
+		for (int o = 1; o < 32; o <<= 1) {
+			const int u = __shfl_up_sync(kFull, incl, o);
+			if (lane >= o) incl += u;
+		}
+		const int excl = incl - v0 - v1;
+		if (lane == 0) s_pre[0] = 0;
+		s_pre[t0 + 1] = excl + v0;
+		s_pre[t1 + 1] = excl + v0 + v1;
+	}
+	__syncthreads();
+	return s_pre[B.n];
+}
+
+// Adds a warp's candidate counts to its image's counters and the launch's
+// total, and clears them.
+__device__ __forceinline__ void pm_batch_count(unsigned long long *image, unsigned long long *total, unsigned &evals,
+                                               unsigned &partial)
+{
+	if ((threadIdx.x & 31) == 0 && evals) {
+		atomicAdd(total, (unsigned long long)evals);
+		if (partial) atomicAdd(total + 1, (unsigned long long)partial);
+		if (image) {
+			atomicAdd(image, (unsigned long long)evals);
+			if (partial) atomicAdd(image + 1, (unsigned long long)partial);
+		}
+	}
+	evals = partial = 0;
+}
+
+// The padded float4 pixels of every active image (k_pad4 per image).
+__global__ void k_pad4_batch(const __grid_constant__ PmBatchArgs B, int C)
+{
+	const int t = blockIdx.y;
+	const PmBatchTask &T = B.t[t];
+	if (!batch_on(B.active, T.flag)) return;
+	pad4_span(T.img, T.p.sW, T.p.sH, C, const_cast<float4 *>(T.p.src), blockIdx.x * blockDim.x + threadIdx.x,
+	          gridDim.x * blockDim.x);
+}
+
+// k_fill_nnf per active image: the result field to "none", and the image's
+// call index advanced when it has target points.
+__global__ void k_fill_nnf_batch(const __grid_constant__ PmBatchArgs B)
+{
+	const int t = blockIdx.y;
+	const PmBatchTask &T = B.t[t];
+	if (!batch_on(B.active, T.flag)) return;
+	if (T.p.nt > 0 && blockIdx.x == 0 && threadIdx.x == 0) *const_cast<unsigned long long *>(T.p.calls) += 1ull;
+	const int n = T.p.tW * T.p.tH;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+		T.nnf_x[i] = make_int2(-1, -1);
+}
+
+template <int KIND, int C, int P>
+__global__ void __launch_bounds__(pm_threads(kPmShared), 1)
+    k_pm_init_batch(DistArgs a, const __grid_constant__ PmBatchArgs B, unsigned long long *counter)
+{
+	__shared__ int s_pre[kBatchMax + 1];
+	const int lane = threadIdx.x & 31;
+	const PmSmem m = pm_smem<kPmShared>(a, B.t[0].p);
+	TmaState ts = {nullptr, nullptr, 0, nullptr, 0u, nullptr};
+	float4 tw[1];
+	load_weights(a, m.w);
+	const int total = pm_batch_prefix(B, s_pre);
+	unsigned evals = 0, partial = 0;
+	const int chunk = (total + gridDim.x - 1) / gridDim.x;
+	const int end = min(total, (int)(blockIdx.x + 1) * chunk);
+	int t = 0, tk = -1;
+	uint2 key = make_uint2(0u, 0u);
+	for (int wi = blockIdx.x * chunk + (threadIdx.x >> 5); wi < end; wi += blockDim.x >> 5) {
+		while (wi >= s_pre[t + 1]) t++;
+		const PmBatchTask &T = B.t[t];
+		if (t != tk) {
+			if (tk >= 0) pm_batch_count(B.t[tk].counter, counter, evals, partial);
+			key = pm_key(T.p);
+			tk = t;
+		}
+		pm_init_point<KIND, C, P, kPmShared>(T.p, m, ts, tw, key, T.p.tlist[wi - s_pre[t]], T.init, T.nnf_x,
+		                                     T.dist_x, evals, partial);
+	}
+	if (tk >= 0) pm_batch_count(B.t[tk].counter, counter, evals, partial);
+}
+
+template <int KIND, int C, int P>
+__global__ void __launch_bounds__(pm_threads(kPmShared), 1)
+    k_pm_sweep_batch(DistArgs a, const __grid_constant__ PmBatchArgs B, int sweep, unsigned long long *counter)
+{
+	__shared__ int s_pre[kBatchMax + 1];
+	const int lane = threadIdx.x & 31;
+	const PmSmem m = pm_smem<kPmShared>(a, B.t[0].p);
+	TmaState ts = {nullptr, nullptr, 0, nullptr, 0u, nullptr};
+	float4 tw[1];
+	load_weights(a, m.w);
+	const int total = pm_batch_prefix(B, s_pre);
+	unsigned evals = 0, partial = 0, improved = 0;
+	int max_shot = -1;
+	const bool even = (sweep % 2) == 0;
+	const int chunk = (total + gridDim.x - 1) / gridDim.x;
+	const int end = min(total, (int)(blockIdx.x + 1) * chunk);
+	int t = 0, tk = -1, windows = 0, jump = 1;
+	uint2 key = make_uint2(0u, 0u);
+	for (int wi = blockIdx.x * chunk + (threadIdx.x >> 5); wi < end; wi += blockDim.x >> 5) {
+		while (wi >= s_pre[t + 1]) t++;
+		const PmBatchTask &T = B.t[t];
+		if (t != tk) {
+			if (tk >= 0) pm_batch_count(B.t[tk].counter, counter, evals, partial);
+			key = pm_key(T.p);
+			windows = 32 - __clz(T.p.max_window);
+			jump = jump_for(sweep, T.p.tW, T.p.tH);
+			tk = t;
+		}
+		pm_sweep_point<KIND, C, P, kPmShared>(T.p, m, ts, tw, key, windows, T.p.tlist[wi - s_pre[t]], sweep, jump,
+		                                      even ? T.nnf_x : T.nnf_y, even ? T.dist_x : T.dist_y,
+		                                      even ? T.nnf_y : T.nnf_x, even ? T.dist_y : T.dist_x, evals, partial,
+		                                      improved, max_shot);
+	}
+	if (tk >= 0) pm_batch_count(B.t[tk].counter, counter, evals, partial);
+}
+
+// After an odd number of sweeps the field is in the second buffer: copy
+// the target points back (k_copy_targets per active image).
+__global__ void k_copy_targets_batch(const __grid_constant__ PmBatchArgs B)
+{
+	const int t = blockIdx.y;
+	const PmBatchTask &T = B.t[t];
+	if (!batch_on(B.active, T.flag)) return;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < T.p.nt; i += gridDim.x * blockDim.x) {
+		const int pix = T.p.tlist[i];
+		T.nnf_x[pix] = T.nnf_y[pix];
+	}
+}
+
+template <int KIND, int C, int P>
+static void run_batch_kernels(nli_ctx *ctx, const DistArgs &a, const PmBatchArgs &B, int iterations, size_t smem,
+                              unsigned long long *counter)
+{
+	// dynamic shared memory up to the opt-in limit less the kernels' static
+	// shared memory (the work-list prefix), raised once per device
+	static std::atomic<uint32_t> raised{0};  // one bit per device
+	static int dyn_max[32];
+	const uint32_t bit = 1u << (ctx->device & 31);
+	if (!(raised.load(std::memory_order_acquire) & bit)) {
+		cudaFuncAttributes fa_init, fa_sweep;
+		NLI_CUDA(cudaFuncGetAttributes(&fa_init, k_pm_init_batch<KIND, C, P>));
+		NLI_CUDA(cudaFuncGetAttributes(&fa_sweep, k_pm_sweep_batch<KIND, C, P>));
+		const int dmax = ctx->max_smem_optin - (int)std::max(fa_init.sharedSizeBytes, fa_sweep.sharedSizeBytes);
+		NLI_CUDA(cudaFuncSetAttribute(k_pm_init_batch<KIND, C, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmax));
+		NLI_CUDA(cudaFuncSetAttribute(k_pm_sweep_batch<KIND, C, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmax));
+		dyn_max[ctx->device & 31] = dmax;
+		raised.fetch_or(bit, std::memory_order_release);
+	}
+	NLI_REQUIRE(smem <= (size_t)dyn_max[ctx->device & 31], NLI_E_UNSUPPORTED, "PatchMatch shared memory too large");
+	const int block = pm_threads(kPmShared);
+	const int grid = ctx->num_sms;
+	{
+		ProfScope ps(ctx, "pm_init");
+		k_pm_init_batch<KIND, C, P><<<grid, block, smem, ctx->stream>>>(a, B, counter);
+		NLI_CHECK_LAUNCH();
+	}
+	for (int it = 0; it < iterations; it++) {
+		ProfScope ps(ctx, "pm_sweep");
+		k_pm_sweep_batch<KIND, C, P><<<grid, block, smem, ctx->stream>>>(a, B, it, counter);
+		NLI_CHECK_LAUNCH();
+	}
+}
+
+void patchmatch_batch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patchmatch_params &pm, int C, int n,
+                          const PmBatchItem *items, const int *active)
+{
+	NLI_REQUIRE(n >= 1 && n <= kBatchMax, NLI_E_INVALID, "batched PatchMatch takes 1 to 64 images");
+	DistArgs a;
+	fill_dist_args(a, dp, C);
+	const bool grad = dp.kind == NLI_DIST_L2_COMBINED || dp.kind == NLI_DIST_L2_RGBD;
+	PmBatchArgs B;
+	std::memset(&B, 0, sizeof(B));
+	B.n = n;
+	B.active = active;
+	int maxpix = 0, maxpad = 0, maxnt = 0;
+	for (int i = 0; i < n; i++) {
+		const PmBatchItem &it = items[i];
+		NLI_REQUIRE(it.W < 32768 && it.H < 32768, NLI_E_UNSUPPORTED, "PatchMatch source sides must be below 32768");
+		PmBatchTask &T = B.t[i];
+		PmArgs &p = T.p;
+		p.src = p.tgt = it.pad;
+		p.sWp = p.tWp = it.W + 1;
+		p.smask = it.smask;
+		p.tmask = it.tmask;
+		p.tlist = it.tlist;
+		p.sW = p.tW = it.W;
+		p.sH = p.tH = it.H;
+		p.nt = it.nt;
+		p.shots = pm.random_shots;
+		p.max_window = (pm.window != -1) ? pm.window : max(it.W, it.H);
+		p.rx = a.rx;
+		p.ry = a.ry;
+		p.ex = a.px - a.rx;
+		p.ey = a.py - a.ry;
+		p.L = a.px + (grad ? 1 : 0);
+		p.K = 32 / p.L;
+		p.rows = a.py + (grad ? 1 : 0);
+		p.lambda = a.lambda;
+		p.lambda_d = a.lambda_d;
+		p.seed = it.seed;
+		p.calls = it.calls;
+		T.flag = it.flag;
+		T.counter = it.counter;
+		T.img = it.img;
+		T.init = reinterpret_cast<const int2 *>(it.init);
+		T.nnf_x = reinterpret_cast<int2 *>(it.out);
+		T.nnf_y = reinterpret_cast<int2 *>(it.nnf_y);
+		T.dist_x = it.dist_x;
+		T.dist_y = it.dist_y;
+		maxpix = max(maxpix, it.W * it.H);
+		maxpad = max(maxpad, (it.W + 1) * (it.H + 1));
+		maxnt = max(maxnt, it.nt);
+	}
+	cudaStream_t s = ctx->stream;
+	const int per = 256;
+	k_pad4_batch<<<dim3((unsigned)std::min((maxpad + per - 1) / per, 1024), (unsigned)n), per, 0, s>>>(B, C);
+	NLI_CHECK_LAUNCH();
+	k_fill_nnf_batch<<<dim3((unsigned)std::min((maxpix + per - 1) / per, 1024), (unsigned)n), per, 0, s>>>(B);
+	NLI_CHECK_LAUNCH();
+	if (maxnt == 0) return;
+	unsigned long long *counter = ctx->buf<unsigned long long>("pm.counter", 2);
+	const int taps = a.px * a.py;
+	const size_t smem = pm_smem_bytes(taps, B.t[0].p.rows, B.t[0].p.L, pm_threads(kPmShared) / 32);
+	NLI_REQUIRE(smem <= (size_t)ctx->max_smem_optin, NLI_E_UNSUPPORTED, "PatchMatch shared memory too large");
+	const bool p9 = a.px == 9 && a.py == 9;
+	bool handled = false;
+#define NLI_PMB_CASE(KIND, CC)                                                                  \
+	if (dp.kind == KIND && C == CC) {                                                           \
+		if (p9)                                                                                 \
+			run_batch_kernels<KIND, CC, 9>(ctx, a, B, pm.iterations, smem, counter);          \
+		else                                                                                    \
+			run_batch_kernels<KIND, CC, 0>(ctx, a, B, pm.iterations, smem, counter);          \
+		handled = true;                                                                         \
+	}
+	NLI_PMB_CASE(NLI_DIST_L2_COMBINED, 3)
+	NLI_PMB_CASE(NLI_DIST_L2_COMBINED, 1)
+	NLI_PMB_CASE(NLI_DIST_L2_COMBINED, 2)
+	NLI_PMB_CASE(NLI_DIST_L2_COMBINED, 4)
+	NLI_PMB_CASE(NLI_DIST_L2_RGBD, 4)
+	NLI_PMB_CASE(NLI_DIST_L2_NORM, 3)
+	NLI_PMB_CASE(NLI_DIST_L2_NORM, 1)
+	NLI_PMB_CASE(NLI_DIST_L2_NORM, 2)
+	NLI_PMB_CASE(NLI_DIST_L2_NORM, 4)
+	NLI_PMB_CASE(NLI_DIST_L1_NORM, 3)
+	NLI_PMB_CASE(NLI_DIST_L1_NORM, 1)
+	NLI_PMB_CASE(NLI_DIST_L1_NORM, 2)
+	NLI_PMB_CASE(NLI_DIST_L1_NORM, 4)
+#undef NLI_PMB_CASE
+	NLI_REQUIRE(handled, NLI_E_UNSUPPORTED, "no PatchMatch kernel for this distance / channel count");
+	if (pm.iterations % 2 == 1) {
+		k_copy_targets_batch<<<dim3((unsigned)std::min((maxnt + per - 1) / per, 1024), (unsigned)n), per, 0, s>>>(B);
+		NLI_CHECK_LAUNCH();
+	}
+}
+
+NLI_CHECK_READER(check_word_patchmatch)
 
 void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patchmatch_params &pm, const float *src,
                     const uint8_t *smask, int sW, int sH, const float *tgt, const uint8_t *tmask, int tW, int tH,

@@ -10,6 +10,8 @@
 //              per-channel lambda on the 4-channel image, orig = image
 #include <cooperative_groups.h>
 
+#include <atomic>
+
 #include "nli_device.cuh"
 
 namespace nli {
@@ -41,6 +43,49 @@ static void fill_upd_args(UpdArgs &u, const nli_update_params &p, int W, int H, 
 // weight indexed from the clipped window corner (:71), confidence applied
 // inside the domain only (:72-74).  New values go to a compact buffer and
 // are scattered afterwards, so every pixel reads the pre-update image.
+// One hole pixel: the new values into out[0..C) and (u_old - u_new)^2
+// summed over the channels.  u supplies the patch and its weights; W, H,
+// C are the image's.
+__device__ __forceinline__ double nlmeans_pixel(const UpdArgs &u, int W, int H, int C, const float *__restrict__ img,
+                                                int pix, const uint8_t *__restrict__ dom, const int2 *__restrict__ nnf,
+                                                const float *__restrict__ conf, float *__restrict__ out)
+{
+	double acc = 0.0;
+	if (!nli_in_bounds(pix, (long long)W * H, kSiteHole)) return 0.0;
+	const int x = pix % W, y = pix / W;
+	const int x_a = max(x - u.hx, 0), x_b = min(x + u.hx, W - 1);
+	const int y_a = max(y - u.hy, 0), y_b = min(y + u.hy, H - 1);
+	float tv[4] = {0.f, 0.f, 0.f, 0.f};
+	float tw = 0.f;
+	for (int ii = x_a; ii <= x_b; ii++)
+		for (int jj = y_a; jj <= y_b; jj++) {
+			int2 q = nnf[jj * W + ii];
+			if (q.x != -1) {
+				q.x += x - ii;
+				q.y += y - jj;
+				if (q.x >= 0 && q.y >= 0 && q.x < W && q.y < H &&
+				    nli_in_bounds((long long)q.y * W + q.x, (long long)W * H, kSiteMeansSource)) {
+					float w = u.weights[(jj - y_a) * u.px + (ii - x_a)];
+					if (conf && dom[jj * W + ii]) w = fm(w, conf[jj * W + ii]);
+					tw = fa(tw, w);
+					const float *s = img + (size_t)C * (q.y * W + q.x);
+					for (int c = 0; c < C; c++) tv[c] = fa(tv[c], fm(s[c], w));
+				}
+			}
+		}
+	for (int c = 0; c < C; c++) {
+		const float prev = img[(size_t)C * pix + c];
+		float v = prev;
+		if (tw > 0.0f) {
+			v = __fdiv_rn(tv[c], tw);
+			const float d = fs(prev, v);
+			acc += (double)fm(d, d);
+		}
+		out[c] = v;
+	}
+	return acc;
+}
+
 __global__ void __launch_bounds__(256) k_nlmeans(UpdArgs u, const float *__restrict__ img,
                                                  const int32_t *__restrict__ hole, int nh,
                                                  const uint8_t *__restrict__ dom, const int2 *__restrict__ nnf,
@@ -50,40 +95,7 @@ __global__ void __launch_bounds__(256) k_nlmeans(UpdArgs u, const float *__restr
 	__shared__ double red[8];
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	double acc = 0.0;
-	if (i < nh) {
-		const int W = u.W, H = u.H, C = u.C;
-		const int pix = hole[i];
-		const int x = pix % W, y = pix / W;
-		const int x_a = max(x - u.hx, 0), x_b = min(x + u.hx, W - 1);
-		const int y_a = max(y - u.hy, 0), y_b = min(y + u.hy, H - 1);
-		float tv[4] = {0.f, 0.f, 0.f, 0.f};
-		float tw = 0.f;
-		for (int ii = x_a; ii <= x_b; ii++)
-			for (int jj = y_a; jj <= y_b; jj++) {
-				int2 q = nnf[jj * W + ii];
-				if (q.x != -1) {
-					q.x += x - ii;
-					q.y += y - jj;
-					if (q.x >= 0 && q.y >= 0 && q.x < W && q.y < H) {
-						float w = u.weights[(jj - y_a) * u.px + (ii - x_a)];
-						if (conf && dom[jj * W + ii]) w = fm(w, conf[jj * W + ii]);
-						tw = fa(tw, w);
-						const float *s = img + (size_t)C * (q.y * W + q.x);
-						for (int c = 0; c < C; c++) tv[c] = fa(tv[c], fm(s[c], w));
-					}
-				}
-			}
-		for (int c = 0; c < C; c++) {
-			const float prev = img[(size_t)C * pix + c];
-			float v = prev;
-			if (tw > 0.0f) {
-				v = __fdiv_rn(tv[c], tw);
-				const float d = fs(prev, v);
-				acc += (double)fm(d, d);
-			}
-			newval[(size_t)C * i + c] = v;
-		}
-	}
+	if (i < nh) acc = nlmeans_pixel(u, u.W, u.H, u.C, img, hole[i], dom, nnf, conf, newval + (size_t)u.C * i);
 	acc = block_sum<256>(acc, red);
 	if (threadIdx.x == 0) partials[blockIdx.x] = acc;
 }
@@ -104,6 +116,105 @@ __global__ void k_scatter_values(const int32_t *__restrict__ hole, int nh, int C
 // shared memory in sorted order, and the weighted median is found by the
 // reference's sequential subtraction (:110-127) in lane 0.
 constexpr int kMedWarps = 4;
+
+// Shared memory of one NL-medians warp.
+struct MedSmem {
+	float (*val)[kMaxTaps];  // [4][kMaxTaps] candidate values per channel
+	float *w, *sv, *sw;       // weights, sorted values, their weights
+};
+
+// One hole pixel, computed by one whole warp: lane 0 writes the new values
+// into out[0..C) and returns (u_old - u_new)^2 summed over the channels.
+__device__ __forceinline__ double nlmedians_pixel(const UpdArgs &u, int W, int H, int C,
+                                                  const float *__restrict__ img, int pix,
+                                                  const uint8_t *__restrict__ dom, const int2 *__restrict__ nnf,
+                                                  const float *__restrict__ conf, float *__restrict__ out, MedSmem sm)
+{
+	const int lane = threadIdx.x & 31;
+	double acc = 0.0;
+	if (!nli_in_bounds(pix, (long long)W * H, kSiteHole)) return 0.0;
+	const int x = pix % W, y = pix / W;
+	const int x_a = max(x - u.hx, 0), x_b = min(x + u.hx, W - 1);
+	const int y_a = max(y - u.hy, 0), y_b = min(y + u.hy, H - 1);
+	const int ny = y_b - y_a + 1;
+	const int total = (x_b - x_a + 1) * ny;
+	// collect valid candidates in reference order (compacted)
+	int m = 0;
+	for (int base = 0; base < total; base += 32) {
+		const int k = base + lane;
+		bool valid = false;
+		float w = 0.f;
+		int qx = 0, qy = 0;
+		if (k < total) {
+			const int ii = x_a + k / ny, jj = y_a + k % ny;
+			int2 q = nnf[jj * W + ii];
+			if (q.x != -1) {
+				qx = q.x + x - ii;
+				qy = q.y + y - jj;
+				if (qx >= 0 && qy >= 0 && qx < W && qy < H &&
+				    nli_in_bounds((long long)qy * W + qx, (long long)W * H, kSiteMeansSource)) {
+					valid = true;
+					w = u.weights[(jj - y_a) * u.px + (ii - x_a)];
+					if (conf && dom[jj * W + ii]) w = fm(w, conf[jj * W + ii]);
+				}
+			}
+		}
+		const unsigned bal = __ballot_sync(0xffffffffu, valid);
+		if (valid) {
+			const int slot = m + __popc(bal & ((1u << lane) - 1u));
+			sm.w[slot] = w;
+			for (int c = 0; c < C; c++) sm.val[c][slot] = img[(size_t)C * (qy * W + qx) + c];
+		}
+		m += __popc(bal);
+	}
+	__syncwarp();
+	if (m > 0) {
+		// total weight, summed in candidate order (:80)
+		float tw = 0.f;
+		if (lane == 0)
+			for (int k = 0; k < m; k++) tw = fa(tw, sm.w[k]);
+		tw = __shfl_sync(0xffffffffu, tw, 0);
+		for (int c = 0; c < C; c++) {
+			for (int k = lane; k < m; k += 32) {
+				const float v = sm.val[c][k];
+				int rank = 0;
+				for (int j = 0; j < m; j++) {
+					const float o = sm.val[c][j];
+					rank += (o < v || (o == v && j < k)) ? 1 : 0;
+				}
+				sm.sv[rank] = v;
+				sm.sw[rank] = sm.w[k];
+			}
+			__syncwarp();
+			if (lane == 0) {
+				float median = 0.0f;
+				float t = tw;
+				const float half = tw / 2;
+				for (int k = 0; k < m; k++) {
+					t = fs(t, sm.sw[k]);
+					if (t < half) {
+						median = sm.sv[k];
+						break;
+					}
+				}
+				const float prev = img[(size_t)C * pix + c];
+				const float d = fs(prev, median);
+				acc += (double)fm(d, d);
+				out[c] = median;
+			}
+			__syncwarp();
+		}
+	} else if (lane == 0) {
+		for (int c = 0; c < C; c++) out[c] = img[(size_t)C * pix + c];
+	}
+	return acc;
+}
+
+// One warp per hole pixel: the candidates of the 9x9 window are numbered
+// in the reference's order (x outer, y inner, :61-62), ranked by value per
+// channel with a warp-wide comparison (ties by candidate order), placed in
+// shared memory in sorted order, and the weighted median is found by the
+// reference's sequential subtraction (:110-127) in lane 0.
 __global__ void __launch_bounds__(32 * kMedWarps) k_nlmedians(UpdArgs u, const float *__restrict__ img,
                                                               const int32_t *__restrict__ hole, int nh,
                                                               const uint8_t *__restrict__ dom,
@@ -119,83 +230,9 @@ __global__ void __launch_bounds__(32 * kMedWarps) k_nlmedians(UpdArgs u, const f
 	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 	const int i = blockIdx.x * kMedWarps + wid;
 	double acc = 0.0;
-	if (i < nh) {
-		const int W = u.W, H = u.H, C = u.C;
-		const int pix = hole[i];
-		const int x = pix % W, y = pix / W;
-		const int x_a = max(x - u.hx, 0), x_b = min(x + u.hx, W - 1);
-		const int y_a = max(y - u.hy, 0), y_b = min(y + u.hy, H - 1);
-		const int ny = y_b - y_a + 1;
-		const int total = (x_b - x_a + 1) * ny;
-		// collect valid candidates in reference order (compacted)
-		int m = 0;
-		for (int base = 0; base < total; base += 32) {
-			const int k = base + lane;
-			bool valid = false;
-			float w = 0.f;
-			int qx = 0, qy = 0;
-			if (k < total) {
-				const int ii = x_a + k / ny, jj = y_a + k % ny;
-				int2 q = nnf[jj * W + ii];
-				if (q.x != -1) {
-					qx = q.x + x - ii;
-					qy = q.y + y - jj;
-					if (qx >= 0 && qy >= 0 && qx < W && qy < H) {
-						valid = true;
-						w = u.weights[(jj - y_a) * u.px + (ii - x_a)];
-						if (conf && dom[jj * W + ii]) w = fm(w, conf[jj * W + ii]);
-					}
-				}
-			}
-			const unsigned bal = __ballot_sync(0xffffffffu, valid);
-			if (valid) {
-				const int slot = m + __popc(bal & ((1u << lane) - 1u));
-				s_w[wid][slot] = w;
-				for (int c = 0; c < C; c++) s_val[wid][c][slot] = img[(size_t)C * (qy * W + qx) + c];
-			}
-			m += __popc(bal);
-		}
-		__syncwarp();
-		if (m > 0) {
-			// total weight, summed in candidate order (:80)
-			float tw = 0.f;
-			if (lane == 0)
-				for (int k = 0; k < m; k++) tw = fa(tw, s_w[wid][k]);
-			tw = __shfl_sync(0xffffffffu, tw, 0);
-			for (int c = 0; c < C; c++) {
-				for (int k = lane; k < m; k += 32) {
-					const float v = s_val[wid][c][k];
-					int rank = 0;
-					for (int j = 0; j < m; j++) {
-						const float o = s_val[wid][c][j];
-						rank += (o < v || (o == v && j < k)) ? 1 : 0;
-					}
-					s_sv[wid][rank] = v;
-					s_sw[wid][rank] = s_w[wid][k];
-				}
-				__syncwarp();
-				if (lane == 0) {
-					float median = 0.0f;
-					float t = tw;
-					const float half = tw / 2;
-					for (int k = 0; k < m; k++) {
-						t = fs(t, s_sw[wid][k]);
-						if (t < half) {
-							median = s_sv[wid][k];
-							break;
-						}
-					}
-					const float prev = img[(size_t)C * pix + c];
-					const float d = fs(prev, median);
-					acc += (double)fm(d, d);
-					newval[(size_t)C * i + c] = median;
-				}
-				__syncwarp();
-			}
-		} else if (lane == 0) {
-			for (int c = 0; c < C; c++) newval[(size_t)C * i + c] = img[(size_t)C * pix + c];
-		}
-	}
+	if (i < nh)
+		acc = nlmedians_pixel(u, u.W, u.H, u.C, img, hole[i], dom, nnf, conf, newval + (size_t)u.C * i,
+		                      MedSmem{s_val[wid], s_w[wid], s_sv[wid], s_sw[wid]});
 	if (lane == 0) red[wid] = acc;
 	__syncthreads();
 	if (threadIdx.x == 0) {
@@ -221,12 +258,11 @@ struct CoefOut {
 	float *GY;  // W*H*C
 };
 
-__device__ __forceinline__ void gather_coef(const UpdArgs &u, int qx, int qy, const uint8_t *__restrict__ ext,
-                                            const int2 *__restrict__ nnf, const float *__restrict__ conf,
-                                            const float *__restrict__ img, const float2 *__restrict__ grad,
-                                            CoefOut out)
+__device__ __forceinline__ void gather_coef(const UpdArgs &u, int W, int H, int C, int qx, int qy,
+                                            const uint8_t *__restrict__ ext, const int2 *__restrict__ nnf,
+                                            const float *__restrict__ conf, const float *__restrict__ img,
+                                            const float2 *__restrict__ grad, CoefOut out)
 {
-	const int W = u.W, H = u.H, C = u.C;
 	float S = 0.f, U[4] = {0, 0, 0, 0}, GX[4] = {0, 0, 0, 0}, GY[4] = {0, 0, 0, 0};
 	const int cy0 = max(qy - u.hy, 0), cy1 = min(qy + u.hy, H - 1);
 	const int cx0 = max(qx - u.hx, 0), cx1 = min(qx + u.hx, W - 1);
@@ -258,6 +294,23 @@ __device__ __forceinline__ void gather_coef(const UpdArgs &u, int qx, int qy, co
 	}
 }
 
+// Hole pixel k and the neighbours it owns (see k_poisson_coef).
+__device__ __forceinline__ void coef_hole_pixel(const UpdArgs &u, int W, int H, int C, int pix,
+                                                const uint8_t *__restrict__ dom, const uint8_t *__restrict__ ext,
+                                                const int2 *__restrict__ nnf, const float *__restrict__ conf,
+                                                const float *__restrict__ img, const float2 *__restrict__ grad,
+                                                CoefOut out)
+{
+	const int x = pix % W, y = pix / W;
+	gather_coef(u, W, H, C, x, y, ext, nnf, conf, img, grad, out);
+	// left neighbour: owned by this hole pixel when it is not a hole pixel
+	if (x > 0 && !dom[pix - 1]) gather_coef(u, W, H, C, x - 1, y, ext, nnf, conf, img, grad, out);
+	// upper neighbour: owned here when it is neither a hole pixel nor the left
+	// neighbour of a hole pixel (then its right neighbour owns it)
+	if (y > 0 && !dom[pix - W] && !(x + 1 < W && dom[pix - W + 1]))
+		gather_coef(u, W, H, C, x, y - 1, ext, nnf, conf, img, grad, out);
+}
+
 __global__ void __launch_bounds__(128) k_poisson_coef(UpdArgs u, const int32_t *__restrict__ hole, int nh,
                                                       const uint8_t *__restrict__ dom,
                                                       const uint8_t *__restrict__ ext, const int2 *__restrict__ nnf,
@@ -266,37 +319,22 @@ __global__ void __launch_bounds__(128) k_poisson_coef(UpdArgs u, const int32_t *
 {
 	const int i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= nh) return;
-	const int W = u.W;
-	const int pix = hole[i];
-	const int x = pix % W, y = pix / W;
-	gather_coef(u, x, y, ext, nnf, conf, img, grad, out);
-	// left neighbour: owned by this hole pixel when it is not a hole pixel
-	if (x > 0 && !dom[pix - 1]) gather_coef(u, x - 1, y, ext, nnf, conf, img, grad, out);
-	// upper neighbour: owned here when it is neither a hole pixel nor the left
-	// neighbour of a hole pixel (then its right neighbour owns it)
-	if (y > 0 && !dom[pix - W] && !(x + 1 < W && dom[pix - W + 1]))
-		gather_coef(u, x, y - 1, ext, nnf, conf, img, grad, out);
+	coef_hole_pixel(u, u.W, u.H, u.C, hole[i], dom, ext, nnf, conf, img, grad, out);
 }
 
-// The same gather with 8 lanes per coefficient pixel: item (k, which) is
-// hole pixel k itself (which 0), its left neighbour (1) or its upper
-// neighbour (2) when that pixel is owned as in k_poisson_coef; lane j of
-// the item's 8 takes window taps j, j + 8, ...; the 8 partial sums are
-// added with shuffles.  Same terms as gather_coef, summed in a tree.
-__global__ void __launch_bounds__(256) k_poisson_coef8(UpdArgs u, const int32_t *__restrict__ hole, int nh,
-                                                       const uint8_t *__restrict__ dom,
-                                                       const uint8_t *__restrict__ ext, const int2 *__restrict__ nnf,
-                                                       const float *__restrict__ conf, const float *__restrict__ img,
-                                                       const float2 *__restrict__ grad, CoefOut out)
+// Item `item` (thread group of 8 lanes, `sub` = lane within the group).
+__device__ __forceinline__ void coef8_item(const UpdArgs &u, int W, int H, int C, int item, int sub,
+                                           const int32_t *__restrict__ hole, int nh, const uint8_t *__restrict__ dom,
+                                           const uint8_t *__restrict__ ext, const int2 *__restrict__ nnf,
+                                           const float *__restrict__ conf, const float *__restrict__ img,
+                                           const float2 *__restrict__ grad, CoefOut out)
 {
-	const int item = (blockIdx.x * blockDim.x + threadIdx.x) >> 3;
-	const int sub = threadIdx.x & 7;
-	const int W = u.W, H = u.H, C = u.C;
 	bool owned = false;
 	int qx = 0, qy = 0;
 	if (item < 3 * nh) {
 		const int k = item / 3, which = item - 3 * k;
 		const int pix = hole[k];
+		if (!nli_in_bounds(pix, (long long)W * H, kSiteHole)) return;  // the item's 8 lanes leave together
 		const int x = pix % W, y = pix / W;
 		if (which == 0) {
 			owned = true;
@@ -327,6 +365,7 @@ __global__ void __launch_bounds__(256) k_poisson_coef8(UpdArgs u, const int32_t 
 		const int2 nb = nnf[c];
 		const int nx = nb.x + qx - cx, ny = nb.y + qy - cy;
 		if (nx < 0 || ny < 0 || nx >= W || ny >= H) continue;
+		if (!nli_in_bounds((long long)ny * W + nx, (long long)W * H, kSiteCoefSource)) continue;
 		float w = u.weights[t];
 		if (conf) w = conf[c] * w;
 		S += w;
@@ -361,6 +400,21 @@ __global__ void __launch_bounds__(256) k_poisson_coef8(UpdArgs u, const int32_t 
 	}
 }
 
+// The same gather with 8 lanes per coefficient pixel: item (k, which) is
+// hole pixel k itself (which 0), its left neighbour (1) or its upper
+// neighbour (2) when that pixel is owned as in k_poisson_coef; lane j of
+// the item's 8 takes window taps j, j + 8, ...; the 8 partial sums are
+// added with shuffles.  Same terms as gather_coef, summed in a tree.
+__global__ void __launch_bounds__(256) k_poisson_coef8(UpdArgs u, const int32_t *__restrict__ hole, int nh,
+                                                       const uint8_t *__restrict__ dom,
+                                                       const uint8_t *__restrict__ ext, const int2 *__restrict__ nnf,
+                                                       const float *__restrict__ conf, const float *__restrict__ img,
+                                                       const float2 *__restrict__ grad, CoefOut out)
+{
+	coef8_item(u, u.W, u.H, u.C, (blockIdx.x * blockDim.x + threadIdx.x) >> 3, threadIdx.x & 7, hole, nh, dom, ext,
+	           nnf, conf, img, grad, out);
+}
+
 // Per unknown (hole pixel) data of the symmetric system
 //   (a1 - div a2 grad) delta = b,  delta = 0 outside the hole,
 // with the anisotropic Laplacian of calculate_anisotropic_laplacian
@@ -385,13 +439,13 @@ struct PoissonArgs {
 
 // Right-hand side b and initial perturbation delta0 = image - orig
 // (patch_non_local_poisson.cpp:62-82), and the per-unknown system data.
-__global__ void k_poisson_setup(PoissonArgs a, int chunk, const int32_t *__restrict__ hole,
-                                const int32_t *__restrict__ hole_index, CoefOut co, const float *__restrict__ img,
-                                const float *__restrict__ orig, Unknown *__restrict__ unk, float *__restrict__ b,
-                                float *__restrict__ x0)
+__device__ __forceinline__ void poisson_setup_unknown(const PoissonArgs &a, int chunk, int k,
+                                                      const int32_t *__restrict__ hole,
+                                                      const int32_t *__restrict__ hole_index, CoefOut co,
+                                                      const float *__restrict__ img, const float *__restrict__ orig,
+                                                      Unknown *__restrict__ unk, float *__restrict__ b,
+                                                      float *__restrict__ x0)
 {
-	const int k = blockIdx.x * blockDim.x + threadIdx.x;
-	if (k >= a.nh) return;
 	const int W = a.W, H = a.H, C = a.C;
 	const int pix = hole[k];
 	const int x = pix % W, y = pix / W;
@@ -437,6 +491,16 @@ __global__ void k_poisson_setup(PoissonArgs a, int chunk, const int32_t *__restr
 		b[(size_t)c * a.nh + k] = f1 - f2 - a1 * o + lap;
 		x0[(size_t)c * a.nh + k] = img[(size_t)C * pix + c] - o;
 	}
+}
+
+__global__ void k_poisson_setup(PoissonArgs a, int chunk, const int32_t *__restrict__ hole,
+                                const int32_t *__restrict__ hole_index, CoefOut co, const float *__restrict__ img,
+                                const float *__restrict__ orig, Unknown *__restrict__ unk, float *__restrict__ b,
+                                float *__restrict__ x0)
+{
+	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= a.nh) return;
+	poisson_setup_unknown(a, chunk, k, hole, hole_index, co, img, orig, unk, b, x0);
 }
 
 __device__ __forceinline__ float apply_A(const Unknown &n, float lam, const float *__restrict__ v, float vk)
@@ -497,8 +561,11 @@ __global__ void __launch_bounds__(kCgBlock) k_poisson_cg(PoissonArgs a, const Un
                                                          int *__restrict__ iters_out,
                                                          const int32_t *__restrict__ hole,
                                                          const float *orig, float *img,
-                                                         double *__restrict__ diff_part)
+                                                         double *__restrict__ diff_part,
+                                                         const int *__restrict__ active_flag)
 {
+	// a batch image that has stopped iterating: every block leaves at once
+	if (active_flag && *active_flag == 0) return;
 	__shared__ double red[kCgBlock / 32][8];
 	__shared__ double tot[8];
 	const int nh = a.nh, C = a.C;
@@ -683,10 +750,9 @@ struct UnkC {
 	uint32_t links;  // bit 0: down link inside the image, bit 1: right link inside the image
 };
 
-__global__ void k_poisson_compact(const Unknown *__restrict__ unk, int nh, int chunk, UnkC *__restrict__ out)
+__device__ __forceinline__ void poisson_compact_unknown(const Unknown *__restrict__ unk, int k, int chunk,
+                                                        UnkC *__restrict__ out)
 {
-	const int k = blockIdx.x * blockDim.x + threadIdx.x;
-	if (k >= nh) return;
 	const Unknown n = unk[k];
 	auto code = [chunk](int m) -> uint32_t {
 		return (m >= 0) ? (uint32_t)(((m / chunk) << 12) | (m % chunk)) : (uint32_t)kNoNb;
@@ -699,6 +765,13 @@ __global__ void k_poisson_compact(const Unknown *__restrict__ unk, int nh, int c
 	c.lr = (code(n.n_left) << 16) | code(n.n_right);
 	c.links = (uint32_t)n.links;
 	out[k] = c;
+}
+
+__global__ void k_poisson_compact(const Unknown *__restrict__ unk, int nh, int chunk, UnkC *__restrict__ out)
+{
+	const int k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= nh) return;
+	poisson_compact_unknown(unk, k, chunk, out);
 }
 
 // 1 / the diagonal of an unknown's row, lam S + (1 - lam) (sum of its four
@@ -717,16 +790,51 @@ __device__ __forceinline__ float jacobi_inv(const UnkC &n, float lam)
 // true residual, so the solve ends at the same residual as the plain CG,
 // in fewer iterations.  Without PRE, z is r itself and the iteration is the
 // reference's.
-template <int C, bool PRE>
-__global__ void __launch_bounds__(kClusterBlock, 1)
-    k_poisson_cg_cluster(PoissonArgs a, int chunk, const UnkC *__restrict__ unk_g, const float *__restrict__ b,
-                         const float *__restrict__ x0, int *__restrict__ iters_out, const int32_t *__restrict__ hole,
-                         const float *orig, float *img, double *__restrict__ diff_part)
+// The CTAs that solve one system: a thread-block cluster (barriers and
+// distributed shared memory), or one CTA on its own (block barriers, its
+// own shared memory) for systems of at most kClusterMaxChunk unknowns.  The
+// one-CTA form performs the same arithmetic in the same order as a
+// cluster of one CTA.
+template <bool SINGLE>
+struct CgTeam;
+
+template <>
+struct CgTeam<true> {
+	__device__ int rank() const { return 0; }
+	__device__ int size() const { return 1; }
+	__device__ void sync() { __syncthreads(); }
+	template <class T>
+	__device__ T *map(T *p, int) const
+	{
+		return p;
+	}
+};
+
+template <>
+struct CgTeam<false> {
+	cooperative_groups::cluster_group c;
+	__device__ CgTeam() : c(cooperative_groups::this_cluster()) {}
+	__device__ int rank() const { return (int)c.block_rank(); }
+	__device__ int size() const { return (int)c.num_blocks(); }
+	__device__ void sync() { c.sync(); }
+	template <class T>
+	__device__ T *map(T *p, int r)
+	{
+		return c.map_shared_rank(p, r);
+	}
+};
+
+// The solve of channel group `group` (channels [group * C, (group + 1) * C)
+// of the a.C-channel image) by the team's CTAs.
+template <int C, bool PRE, bool SINGLE>
+__device__ __forceinline__ void cg_team_solve(const PoissonArgs &a, int chunk, const UnkC *__restrict__ unk_g,
+                                              const float *__restrict__ b, const float *__restrict__ x0,
+                                              int *__restrict__ iters_out, const int32_t *__restrict__ hole,
+                                              const float *orig, float *img, double *__restrict__ diff_part, int group)
 {
 	constexpr int NV = PRE ? 2 * C : C;  // sums of the residual phase: |r|^2 (and <r, z>)
 	const int Ctot = a.C;
-	namespace cgs = cooperative_groups;
-	cgs::cluster_group cluster = cgs::this_cluster();
+	CgTeam<SINGLE> cluster;
 	extern __shared__ float smem[];
 	__shared__ double red[kClusterBlock / 32][8];
 	__shared__ double partA[8], partB[8], tot[8];
@@ -734,8 +842,8 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 	__shared__ int s_active[4];
 	__shared__ double s_nr[4], s_rho[4];
 	__shared__ float *base[3][kClusterMax];  // z (r without PRE), dA, dB of every CTA
-	const int rank = (int)cluster.block_rank(), ncta = (int)cluster.num_blocks();
-	const int group = (int)blockIdx.x / ncta, cb = group * C;  // this cluster's first channel
+	const int rank = cluster.rank(), ncta = cluster.size();
+	const int cb = group * C;  // this cluster's first channel
 	b += (size_t)cb * a.nh;
 	x0 += (size_t)cb * a.nh;
 	const int nh = a.nh;
@@ -746,9 +854,9 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 	float *s_z = PRE ? smem + 4 * vlen : s_r;
 	UnkC *s_unk = reinterpret_cast<UnkC *>(smem + (kClusterVectors + (PRE ? 1 : 0)) * vlen);
 	if (threadIdx.x < ncta) {
-		base[0][threadIdx.x] = cluster.map_shared_rank(s_z, (int)threadIdx.x);
-		base[1][threadIdx.x] = cluster.map_shared_rank(s_dA, (int)threadIdx.x);
-		base[2][threadIdx.x] = cluster.map_shared_rank(s_dB, (int)threadIdx.x);
+		base[0][threadIdx.x] = cluster.map(s_z, (int)threadIdx.x);
+		base[1][threadIdx.x] = cluster.map(s_dA, (int)threadIdx.x);
+		base[2][threadIdx.x] = cluster.map(s_dB, (int)threadIdx.x);
 	}
 	for (int l = threadIdx.x; l < own; l += blockDim.x) s_unk[l] = unk_g[lo + l];
 	__syncthreads();
@@ -778,7 +886,7 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 #pragma unroll
 		for (int c = 0; c < NV; c++) {
 			if (c >= nv) break;
-			const double v = warp_sum((lane < ncta) ? cluster.map_shared_rank(const_cast<double *>(src), lane)[c] : 0.0);
+			const double v = warp_sum((lane < ncta) ? cluster.map(const_cast<double *>(src), lane)[c] : 0.0);
 			out[c] = __shfl_sync(0xffffffffu, v, 0);
 		}
 	};
@@ -801,8 +909,10 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 		const float sum = coefs[0] + coefs[1] + coefs[2] + coefs[3];
 		int gk[4];
 #pragma unroll
-		for (int j = 0; j < 4; j++)
+		for (int j = 0; j < 4; j++) {
 			gk[j] = (codes[j] != kNoNb) ? (int)(codes[j] >> 12) * chunk + (int)(codes[j] & 0xFFF) : -1;
+			if (gk[j] >= 0 && !nli_in_bounds(gk[j], nh, kSiteCgNeighbour)) gk[j] = -1;
+		}
 #pragma unroll
 		for (int c = 0; c < C; c++) {
 			const float *xc = x0 + (size_t)c * nh;
@@ -869,10 +979,16 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 			const float coefs[4] = {n.s_up, n.s_left, (n.links & 1) ? n.S : 0.f, (n.links & 2) ? n.S : 0.f};
 			const float sum = coefs[0] + coefs[1] + coefs[2] + coefs[3];
 			const float *nr_[4], *nd_[4];
+			bool has[4];
 #pragma unroll
 			for (int j = 0; j < 4; j++) {
-				nr_[j] = (codes[j] != kNoNb) ? nb(0, codes[j]) : nullptr;
-				nd_[j] = (codes[j] != kNoNb) ? nb(1 + h, codes[j]) : nullptr;
+				// a checked build tests the code's owning CTA and index
+				has[j] = codes[j] != kNoNb &&
+				         nli_in_bounds((long long)(codes[j] >> 12) * chunk + (codes[j] & 0xFFF),
+				                       (long long)ncta * chunk, kSiteCgNeighbour) &&
+				         nli_in_bounds(codes[j] & 0xFFF, chunk, kSiteCgNeighbour);
+				nr_[j] = has[j] ? nb(0, codes[j]) : nullptr;
+				nd_[j] = has[j] ? nb(1 + h, codes[j]) : nullptr;
 			}
 #pragma unroll
 			for (int c = 0; c < C; c++) {
@@ -883,7 +999,7 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 				float lap = -dk * sum;
 #pragma unroll
 				for (int j = 0; j < 4; j++)
-					if (codes[j] != kNoNb) lap += coefs[j] * (nr_[j][c] + beta[c] * nd_[j][c]);
+					if (has[j]) lap += coefs[j] * (nr_[j][c] + beta[c] * nd_[j][c]);
 				const float qv = a.lambda[cb + c] * n.S * dk - (1.0f - a.lambda[cb + c]) * lap;
 				dnew[o] = dk;
 				q[u][c] = qv;
@@ -982,6 +1098,27 @@ __global__ void __launch_bounds__(kClusterBlock, 1)
 	cluster.sync();  // no CTA leaves while others may still read its shared memory
 }
 
+template <int C, bool PRE>
+__global__ void __launch_bounds__(kClusterBlock, 1)
+    k_poisson_cg_cluster(PoissonArgs a, int chunk, const UnkC *__restrict__ unk_g, const float *__restrict__ b,
+                         const float *__restrict__ x0, int *__restrict__ iters_out, const int32_t *__restrict__ hole,
+                         const float *orig, float *img, double *__restrict__ diff_part)
+{
+	const int ncta = (int)cooperative_groups::this_cluster().num_blocks();
+	cg_team_solve<C, PRE, false>(a, chunk, unk_g, b, x0, iters_out, hole, orig, img, diff_part,
+	                             (int)blockIdx.x / ncta);
+}
+
+// One CTA per channel (systems of at most kClusterMaxChunk unknowns).
+template <int C, bool PRE>
+__global__ void __launch_bounds__(kClusterBlock, 1)
+    k_poisson_cg_cta(PoissonArgs a, int chunk, const UnkC *__restrict__ unk_g, const float *__restrict__ b,
+                     const float *__restrict__ x0, int *__restrict__ iters_out, const int32_t *__restrict__ hole,
+                     const float *orig, float *img, double *__restrict__ diff_part)
+{
+	cg_team_solve<C, PRE, true>(a, chunk, unk_g, b, x0, iters_out, hole, orig, img, diff_part, (int)blockIdx.x);
+}
+
 __global__ void k_hole_index(const int32_t *__restrict__ hole, int nh, int32_t *__restrict__ index)
 {
 	const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -992,6 +1129,8 @@ __global__ void k_fill_int(int32_t *p, int n, int v)
 {
 	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) p[i] = v;
 }
+
+NLI_CHECK_READER(check_word_update)
 
 static double read_total(nli_ctx *ctx, double *partials, int n, int *cg_iters_dev, int C, int nh = 0)
 {
@@ -1032,9 +1171,71 @@ static void (*cluster_kernel(int CC, bool pre))(PoissonArgs, int, const UnkC *, 
 	                   : k_poisson_cg_cluster<4, false>;
 }
 
+static void (*cta_kernel(int CC, bool pre))(PoissonArgs, int, const UnkC *, const float *, const float *, int *,
+                                            const int32_t *, const float *, float *, double *)
+{
+	if (pre)
+		return (CC == 1)   ? k_poisson_cg_cta<1, true>
+		       : (CC == 2) ? k_poisson_cg_cta<2, true>
+		       : (CC == 3) ? k_poisson_cg_cta<3, true>
+		                   : k_poisson_cg_cta<4, true>;
+	return (CC == 1)   ? k_poisson_cg_cta<1, false>
+	       : (CC == 2) ? k_poisson_cg_cta<2, false>
+	       : (CC == 3) ? k_poisson_cg_cta<3, false>
+	                   : k_poisson_cg_cta<4, false>;
+}
+
 // Vectors of `chunk` floats per channel a cluster CTA keeps in shared
 // memory: r, two direction buffers, x (and z when preconditioned).
 static int cluster_vectors(bool pre) { return kClusterVectors + (pre ? 1 : 0); }
+
+// shared-memory cluster kernel: kClusterVectors vectors x chunk floats per CTA, one cluster per channel
+constexpr size_t kSmemBudget = 216 * 1024;
+
+// Solver layout of a system of nh unknowns per channel: *ncta CTAs of
+// *chunk unknowns each (one CTA with block barriers when *ncta is 1, a
+// cluster when it is more), or *ncta = 0 for the cooperative grid CG.
+static void cg_layout(nli_ctx *ctx, int nh, int *ncta, int *chunk)
+{
+	if (ctx->cg_cluster_max < 0) {
+		// largest cluster the device runs with the biggest shared-memory footprint
+		int maxc = 0;
+		bool ok = true;
+		for (int CC = 1; CC <= 4; CC++)
+			for (int pre = 0; pre < 2; pre++) {
+				ok &= cudaFuncSetAttribute(cluster_kernel(CC, pre), cudaFuncAttributeNonPortableClusterSizeAllowed,
+				                           1) == 0;
+				ok &= cudaFuncSetAttribute(cluster_kernel(CC, pre), cudaFuncAttributeMaxDynamicSharedMemorySize,
+				                           (int)kSmemBudget) == 0;
+				ok &= cudaFuncSetAttribute(cta_kernel(CC, pre), cudaFuncAttributeMaxDynamicSharedMemorySize,
+				                           (int)kSmemBudget) == 0;
+			}
+		if (ok) {
+			cudaLaunchConfig_t qc = {};
+			qc.gridDim = dim3(kClusterMax);
+			qc.blockDim = dim3(kClusterBlock);
+			qc.dynamicSmemBytes = kSmemBudget;
+			if (cudaOccupancyMaxPotentialClusterSize(&maxc, cluster_kernel(4, true), &qc) != cudaSuccess) maxc = 0;
+		}
+		cudaGetLastError();
+		ctx->cg_cluster_max = std::min(maxc, kClusterMax);
+	}
+	*ncta = *chunk = 0;
+	if (ctx->cg_cluster_max >= 1) {
+		const int per = std::max(1, ctx->tune_cg_unknowns_per_cta);
+		*ncta = std::max(1, std::min(std::min(ctx->cg_cluster_max, ctx->tune_cg_cluster_cap), (nh + per - 1) / per));
+		*chunk = (nh + *ncta - 1) / *ncta;
+		if ((size_t)cluster_vectors(ctx->tune_cg_precond) * *chunk * sizeof(float) + *chunk * sizeof(UnkC) >
+		        kSmemBudget ||
+		    *chunk > kClusterMaxChunk)
+			*ncta = *chunk = 0;
+		// small systems: one CTA, block barriers only (NLI_TUNE_CG_SINGLE_MAX)
+		if (nh <= std::min(ctx->tune_cg_single_max, kClusterMaxChunk)) {
+			*ncta = 1;
+			*chunk = nh;
+		}
+	}
+}
 
 // Coefficients (gather), the compact system and its right-hand side b and
 // start x0 = image - orig (patch_non_local_poisson.cpp:36-82).  Chooses the
@@ -1086,38 +1287,8 @@ static PoissonSystem poisson_system(nli_ctx *ctx, const UpdArgs &u, const nli_up
 	P.unk = ctx->buf<Unknown>("poi.unk", nh);
 	P.b = ctx->buf<float>("poi.b", (size_t)nh * C);
 	P.x = ctx->buf<float>("poi.x", (size_t)nh * C);
-	// shared-memory cluster kernel: kClusterVectors vectors x chunk floats per CTA, one cluster per channel
-	constexpr size_t kSmemBudget = 216 * 1024;
-	if (ctx->cg_cluster_max < 0) {
-		// largest cluster the device runs with the biggest shared-memory footprint
-		int maxc = 0;
-		bool ok = true;
-		for (int CC = 1; CC <= 4; CC++)
-			for (int pre = 0; pre < 2; pre++) {
-				ok &= cudaFuncSetAttribute(cluster_kernel(CC, pre), cudaFuncAttributeNonPortableClusterSizeAllowed,
-				                           1) == 0;
-				ok &= cudaFuncSetAttribute(cluster_kernel(CC, pre), cudaFuncAttributeMaxDynamicSharedMemorySize,
-				                           (int)kSmemBudget) == 0;
-			}
-		if (ok) {
-			cudaLaunchConfig_t qc = {};
-			qc.gridDim = dim3(kClusterMax);
-			qc.blockDim = dim3(kClusterBlock);
-			qc.dynamicSmemBytes = kSmemBudget;
-			if (cudaOccupancyMaxPotentialClusterSize(&maxc, cluster_kernel(4, true), &qc) != cudaSuccess) maxc = 0;
-		}
-		cudaGetLastError();
-		ctx->cg_cluster_max = std::min(maxc, kClusterMax);
-	}
-	if (ctx->cg_cluster_max >= 1) {
-		const int per = std::max(1, ctx->tune_cg_unknowns_per_cta);
-		P.ncta = std::max(1, std::min(std::min(ctx->cg_cluster_max, ctx->tune_cg_cluster_cap), (nh + per - 1) / per));
-		P.chunk = (nh + P.ncta - 1) / P.ncta;
-		if ((size_t)cluster_vectors(ctx->tune_cg_precond) * P.chunk * sizeof(float) + P.chunk * sizeof(UnkC) >
-		        kSmemBudget ||
-		    P.chunk > kClusterMaxChunk)
-			P.ncta = P.chunk = 0;
-	}
+
+	cg_layout(ctx, nh, &P.ncta, &P.chunk);
 	{
 		ProfScope ps(ctx, "poisson_setup");
 		k_poisson_setup<<<(nh + 255) / 256, 256, 0, s>>>(pa, P.chunk, hole, hole_index, P.co, image, orig, P.unk,
@@ -1125,6 +1296,61 @@ static PoissonSystem poisson_system(nli_ctx *ctx, const UpdArgs &u, const nli_up
 		NLI_CHECK_LAUNCH();
 	}
 	return P;
+}
+
+// Blocks of the cooperative grid CG for nh unknowns: co-resident, at most
+// one per SM.
+static int grid_cg_blocks(nli_ctx *ctx, int nh)
+{
+	int dev_blocks_per_sm = 0;
+	const bool pre = ctx->tune_cg_precond != 0;
+	const void *kern = pre ? (const void *)k_poisson_cg<true> : (const void *)k_poisson_cg<false>;
+	NLI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&dev_blocks_per_sm, kern, kCgBlock, 0));
+	const int max_blocks = dev_blocks_per_sm * ctx->num_sms;
+	NLI_REQUIRE(max_blocks > 0, NLI_E_CUDA, "conjugate gradient kernel cannot be made resident");
+	int grid = (nh + kCgBlock - 1) / kCgBlock;
+	return std::min(std::max(grid, 1), std::min(max_blocks, ctx->num_sms));
+}
+
+struct GridCgBufs {
+	float *r, *d, *q, *z;  // nh * C each (z only when preconditioned)
+	double *part;          // grid * 16
+};
+
+// The cooperative grid CG of system P on `grid` blocks.  active (may be
+// null): a device flag; 0 makes every block leave at once.
+static void launch_grid_cg(nli_ctx *ctx, const PoissonSystem &P, int grid, const GridCgBufs &g, int *iters,
+                           const int32_t *hole, const float *orig, float *img, double *diff_part, const int *active)
+{
+	cudaStream_t s = ctx->stream;
+	const bool pre = ctx->tune_cg_precond != 0;
+	const void *kern = pre ? (const void *)k_poisson_cg<true> : (const void *)k_poisson_cg<false>;
+	// the grid barrier's counters (the timeout word is left for the
+	// iteration's readback)
+	NLI_CUDA(cudaMemsetAsync(ctx->status, 0, offsetof(DevStatus, timeout), s));
+	DevStatus *st = ctx->status;
+	PoissonArgs pa = P.pa;
+	const Unknown *unk = P.unk;
+	const float *b = P.b;
+	float *x = P.x;
+	float *r = g.r, *d = g.d, *q = g.q, *z = g.z;
+	double *part = g.part;
+	void *args[] = {&pa,   &unk, &b,     &x,    (void *)&r, &d,         &q,         &z,
+	                &part, &st,  &iters, (void *)&hole, &orig, &img, &diff_part, (void *)&active};
+	// cooperative through the launch attribute, which stream capture takes
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim = dim3(grid);
+	cfg.blockDim = dim3(kCgBlock);
+	cfg.dynamicSmemBytes = 0;
+	cfg.stream = s;
+	cudaLaunchAttribute attr[1];
+	attr[0].id = cudaLaunchAttributeCooperative;
+	attr[0].val.cooperative = 1;
+	cfg.attrs = attr;
+	cfg.numAttrs = 1;
+	ProfScope ps(ctx, "poisson_cg");
+	NLI_CUDA(cudaLaunchKernelExC(&cfg, kern, args));
+	nli_count_launch_internal();
 }
 
 // Solves the system from x0 (the CG of :387-477) and writes u = orig + x on
@@ -1142,6 +1368,14 @@ static int poisson_solve(nli_ctx *ctx, PoissonSystem &P, const int32_t *hole, co
 		k_poisson_compact<<<(nh + 255) / 256, 256, 0, s>>>(P.unk, nh, P.chunk, unkc);
 		NLI_CHECK_LAUNCH();
 		double *diff_part = ctx->buf<double>("poi.diff", (size_t)C * P.ncta + 1);
+		if (P.ncta == 1) {
+			// one CTA per channel: no cluster
+			ProfScope ps(ctx, "poisson_cg");
+			cta_kernel(1, pre)<<<C, kClusterBlock, smem, s>>>(P.pa, P.chunk, unkc, P.b, P.x, iters, hole, orig, img,
+			                                                  diff_part);
+			NLI_CHECK_LAUNCH();
+			return C;
+		}
 		cudaLaunchConfig_t cfg = {};
 		cfg.gridDim = dim3(C * P.ncta);
 		cfg.blockDim = dim3(kClusterBlock);
@@ -1160,45 +1394,16 @@ static int poisson_solve(nli_ctx *ctx, PoissonSystem &P, const int32_t *hole, co
 		nli_count_launch_internal();
 		return C * P.ncta;
 	}
-	int dev_blocks_per_sm = 0;
-	const bool pre = ctx->tune_cg_precond != 0;
-	const void *kern = pre ? (const void *)k_poisson_cg<true> : (const void *)k_poisson_cg<false>;
-	NLI_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&dev_blocks_per_sm, kern, kCgBlock, 0));
-	const int max_blocks = dev_blocks_per_sm * ctx->num_sms;
-	NLI_REQUIRE(max_blocks > 0, NLI_E_CUDA, "conjugate gradient kernel cannot be made resident");
-	int grid = (nh + kCgBlock - 1) / kCgBlock;
-	grid = std::min(std::max(grid, 1), std::min(max_blocks, ctx->num_sms));
+	const int grid = grid_cg_blocks(ctx, nh);
 	double *part = ctx->buf<double>("poi.part", (size_t)grid * 16);
 	double *diff_part = ctx->buf<double>("poi.diff", grid + 1);
-	float *r = ctx->buf<float>("poi.r", (size_t)nh * C);
-	float *d = ctx->buf<float>("poi.d", (size_t)nh * C);
-	float *q = ctx->buf<float>("poi.q", (size_t)nh * C);
-	float *z = pre ? ctx->buf<float>("poi.z", (size_t)nh * C) : nullptr;
-	// the grid barrier's counters (the timeout word is left for the
-	// iteration's readback)
-	NLI_CUDA(cudaMemsetAsync(ctx->status, 0, offsetof(DevStatus, timeout), s));
-	DevStatus *st = ctx->status;
-	const Unknown *unk = P.unk;
-	const float *b = P.b;
-	float *x = P.x;
-	void *args[] = {&P.pa, &unk, &b,   &x,     (void *)&r, &d, &q, &z, &part, &st, &iters, (void *)&hole,
-	                &orig, &img, &diff_part};
-	{
-		// cooperative through the launch attribute, which stream capture takes
-		cudaLaunchConfig_t cfg = {};
-		cfg.gridDim = dim3(grid);
-		cfg.blockDim = dim3(kCgBlock);
-		cfg.dynamicSmemBytes = 0;
-		cfg.stream = s;
-		cudaLaunchAttribute attr[1];
-		attr[0].id = cudaLaunchAttributeCooperative;
-		attr[0].val.cooperative = 1;
-		cfg.attrs = attr;
-		cfg.numAttrs = 1;
-		ProfScope ps(ctx, "poisson_cg");
-		NLI_CUDA(cudaLaunchKernelExC(&cfg, kern, args));
-		nli_count_launch_internal();
-	}
+	GridCgBufs g;
+	g.r = ctx->buf<float>("poi.r", (size_t)nh * C);
+	g.d = ctx->buf<float>("poi.d", (size_t)nh * C);
+	g.q = ctx->buf<float>("poi.q", (size_t)nh * C);
+	g.z = ctx->tune_cg_precond ? ctx->buf<float>("poi.z", (size_t)nh * C) : nullptr;
+	g.part = part;
+	launch_grid_cg(ctx, P, grid, g, iters, hole, orig, img, diff_part, nullptr);
 	return grid;
 }
 
@@ -1269,6 +1474,471 @@ double update_run(nli_ctx *ctx, const nli_update_params &up, float *image, const
 		return 0.0;
 	}
 	return read_total(ctx, partials, grid, nullptr, C);
+}
+
+// ======================================================= batched updates
+// The update step of up to kBatchMax images in one launch per kernel (the
+// lockstep batch driver, lockstep.cu).  Each image keeps its own sizes,
+// method, lambda and CG tolerance; the patch and its weights are shared.
+// Every per-pixel / per-unknown value comes from the same device functions
+// as the one-image kernels, and every reduction keeps the one-image
+// partition (blocks of one image never straddle another image; each CG
+// system has the same CTA layout), so each image's result and its sum of
+// (u_old - u_new)^2 equal those of its one-image update bit for bit.
+// Images whose active flag is 0 are skipped.  The per-image arguments
+// travel in kernel parameter space (__grid_constant__ tables).
+struct BTask {
+	int img_index;  // index of the image's active flag
+	int W, H, nh;
+	float *img;
+	const float *orig;
+	const uint8_t *dom, *ext;
+	const int2 *nnf;
+	const float *conf;
+	const int32_t *hole;
+	float *newval;      // NL-means / NL-medians: new values of the hole
+	double *partials;   // NL-means / NL-medians: per-block sums
+	int32_t *hidx;      // NL-Poisson: unknown index per pixel
+	float *grad;
+	CoefOut co;
+	Unknown *unk;
+	UnkC *unkc;
+	float *b, *x;
+	PoissonArgs pa;
+	int chunk, ncta;    // CG layout (ncta 0: grid CG)
+	int *iters;
+	double *diff;       // CG: partial sums of (du)^2
+	int nparts;         // partial sums behind `total`
+	double *total;      // this step's sum of (du)^2
+};
+
+struct BArgs {
+	int n;
+	const int *active;
+	int blk[kBatchMax + 1];  // block prefix of the launch
+	BTask t[kBatchMax];
+};
+
+__device__ __forceinline__ bool btask_on(const BArgs &B, int t) { return !B.active || B.active[B.t[t].img_index]; }
+
+// The task whose block range [blk[t], blk[t + 1]) holds block b.
+__device__ __forceinline__ int task_of_block(const BArgs &B, int b)
+{
+	int lo = 0, hi = B.n;
+	while (hi - lo > 1) {
+		const int mid = (lo + hi) >> 1;
+		if (B.blk[mid] <= b)
+			lo = mid;
+		else
+			hi = mid;
+	}
+	return lo;
+}
+
+__global__ void __launch_bounds__(256) k_nlmeans_batch(UpdArgs u, const __grid_constant__ BArgs B, int C)
+{
+	__shared__ double red[8];
+	const int t = task_of_block(B, blockIdx.x);
+	if (!btask_on(B, t)) return;
+	const BTask &T = B.t[t];
+	const int bl = blockIdx.x - B.blk[t];
+	const int i = bl * 256 + threadIdx.x;
+	double acc = 0.0;
+	if (i < T.nh)
+		acc = nlmeans_pixel(u, T.W, T.H, C, T.img, T.hole[i], T.dom, T.nnf, T.conf, T.newval + (size_t)C * i);
+	acc = block_sum<256>(acc, red);
+	if (threadIdx.x == 0) T.partials[bl] = acc;
+}
+
+__global__ void __launch_bounds__(32 * kMedWarps) k_nlmedians_batch(UpdArgs u, const __grid_constant__ BArgs B, int C)
+{
+	__shared__ float s_val[kMedWarps][4][kMaxTaps];
+	__shared__ float s_w[kMedWarps][kMaxTaps];
+	__shared__ float s_sv[kMedWarps][kMaxTaps];
+	__shared__ float s_sw[kMedWarps][kMaxTaps];
+	__shared__ double red[kMedWarps];
+	const int t = task_of_block(B, blockIdx.x);
+	if (!btask_on(B, t)) return;
+	const BTask &T = B.t[t];
+	const int bl = blockIdx.x - B.blk[t];
+	const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	const int i = bl * kMedWarps + wid;
+	double acc = 0.0;
+	if (i < T.nh)
+		acc = nlmedians_pixel(u, T.W, T.H, C, T.img, T.hole[i], T.dom, T.nnf, T.conf, T.newval + (size_t)C * i,
+		                      MedSmem{s_val[wid], s_w[wid], s_sv[wid], s_sw[wid]});
+	if (lane == 0) red[wid] = acc;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		double tt = 0.0;
+		for (int w = 0; w < kMedWarps; w++) tt += red[w];
+		T.partials[bl] = tt;
+	}
+}
+
+// New values into the image (k_scatter_values per image).
+__global__ void k_scatter_batch(const __grid_constant__ BArgs B, int C)
+{
+	const int t = blockIdx.y;
+	if (!btask_on(B, t)) return;
+	const BTask &T = B.t[t];
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < T.nh * C; i += gridDim.x * blockDim.x) {
+		const int k = i / C, c = i % C;
+		T.img[(size_t)C * T.hole[k] + c] = T.newval[i];
+	}
+}
+
+// The image's sum of (du)^2 from its partial sums (k_sum_partials per
+// image: one 1024-thread block each, the same order).  which 0: the
+// NL-means / NL-medians block sums, 1: the CG partial sums.
+__global__ void __launch_bounds__(1024) k_total_batch(const __grid_constant__ BArgs B, int which)
+{
+	__shared__ double sm[32];
+	const int t = blockIdx.x;
+	if (!btask_on(B, t)) return;
+	const BTask &T = B.t[t];
+	const double *part = which ? T.diff : T.partials;
+	double v = 0.0;
+	for (int i = threadIdx.x; i < T.nparts; i += blockDim.x) v += part[i];
+	v = block_sum<1024>(v, sm);
+	if (threadIdx.x == 0) *T.total = v;
+}
+
+// Unknown index per pixel: -1, then k at hole pixel k.
+__global__ void k_hidx_fill_batch(const __grid_constant__ BArgs B)
+{
+	const int t = blockIdx.y;
+	if (!btask_on(B, t)) return;
+	const BTask &T = B.t[t];
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < T.W * T.H; i += gridDim.x * blockDim.x) T.hidx[i] = -1;
+}
+
+__global__ void k_hidx_set_batch(const __grid_constant__ BArgs B)
+{
+	const int t = blockIdx.y;
+	if (!btask_on(B, t)) return;
+	const BTask &T = B.t[t];
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < T.nh; k += gridDim.x * blockDim.x) T.hidx[T.hole[k]] = k;
+}
+
+__global__ void k_gradient_batch(const __grid_constant__ BArgs B, int C)
+{
+	const int t = blockIdx.y;
+	if (!btask_on(B, t)) return;
+	const BTask &T = B.t[t];
+	gradient_span(T.img, T.W, T.H, C, T.grad, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+}
+
+__global__ void __launch_bounds__(256) k_coef8_batch(UpdArgs u, const __grid_constant__ BArgs B, int C)
+{
+	const int t = task_of_block(B, blockIdx.x);
+	if (!btask_on(B, t)) return;
+	const BTask &T = B.t[t];
+	const int item = (((int)blockIdx.x - B.blk[t]) * 256 + (int)threadIdx.x) >> 3;
+	coef8_item(u, T.W, T.H, C, item, threadIdx.x & 7, T.hole, T.nh, T.dom, T.ext, T.nnf, T.conf, T.img,
+	           reinterpret_cast<const float2 *>(T.grad), T.co);
+}
+
+__global__ void __launch_bounds__(128) k_coef_batch(UpdArgs u, const __grid_constant__ BArgs B, int C)
+{
+	const int t = task_of_block(B, blockIdx.x);
+	if (!btask_on(B, t)) return;
+	const BTask &T = B.t[t];
+	const int i = ((int)blockIdx.x - B.blk[t]) * 128 + (int)threadIdx.x;
+	if (i >= T.nh) return;
+	coef_hole_pixel(u, T.W, T.H, C, T.hole[i], T.dom, T.ext, T.nnf, T.conf, T.img,
+	                reinterpret_cast<const float2 *>(T.grad), T.co);
+}
+
+__global__ void k_setup_batch(const __grid_constant__ BArgs B)
+{
+	const int t = task_of_block(B, blockIdx.x);
+	if (!btask_on(B, t)) return;
+	const BTask &T = B.t[t];
+	const int k = ((int)blockIdx.x - B.blk[t]) * 256 + (int)threadIdx.x;
+	if (k >= T.nh) return;
+	poisson_setup_unknown(T.pa, T.chunk, k, T.hole, T.hidx, T.co, T.img, T.orig, T.unk, T.b, T.x);
+}
+
+__global__ void k_compact_batch(const __grid_constant__ BArgs B)
+{
+	const int t = blockIdx.y;
+	if (!btask_on(B, t)) return;
+	const BTask &T = B.t[t];
+	if (T.ncta == 0) return;
+	for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < T.nh; k += gridDim.x * blockDim.x)
+		poisson_compact_unknown(T.unk, k, T.chunk, T.unkc);
+}
+
+// CG systems of one layout class (the same CTAs per system): system g of
+// the launch is channel g % C of task g / C.
+struct CgTask {
+	int img_index;
+	PoissonArgs a;
+	int chunk;
+	const UnkC *unk;
+	const float *b, *x0;
+	int *iters;
+	const int32_t *hole;
+	const float *orig;
+	float *img;
+	double *diff;
+};
+
+struct CgArgs {
+	int n, C, ncta;
+	const int *active;
+	CgTask t[kBatchMax];
+};
+
+template <bool PRE, bool SINGLE>
+__global__ void __launch_bounds__(kClusterBlock, 1) k_poisson_cg_batch(const __grid_constant__ CgArgs B)
+{
+	const int ncta = SINGLE ? 1 : B.ncta;
+	const int g = (int)blockIdx.x / ncta;
+	const int t = g / B.C, group = g - t * B.C;
+	const CgTask &T = B.t[t];
+	// a stopped image: every CTA of its clusters leaves before any barrier
+	if (B.active && !B.active[T.img_index]) return;
+	cg_team_solve<1, PRE, SINGLE>(T.a, T.chunk, T.unk, T.b, T.x0, T.iters, T.hole, T.orig, T.img, T.diff, group);
+}
+
+static void (*cg_batch_kernel(bool pre, bool single))(CgArgs)
+{
+	if (pre) return single ? k_poisson_cg_batch<true, true> : k_poisson_cg_batch<true, false>;
+	return single ? k_poisson_cg_batch<false, true> : k_poisson_cg_batch<false, false>;
+}
+
+static std::string lk_name(int i, const char *what) { return "lk." + std::to_string(i) + "." + what; }
+
+static int div_up(long long a, int b) { return (int)((a + b - 1) / b); }
+
+// Elementwise launch over n images: blockIdx.y = image, grid-stride in x.
+static dim3 per_image_grid(long long maxcount, int n, int block = 256)
+{
+	return dim3((unsigned)std::max(1, std::min(div_up(maxcount, block), 1024)), (unsigned)n);
+}
+
+void update_batch_run(nli_ctx *ctx, const nli_update_params *ups, int C, int n, const UpdBatchItem *items,
+                      const int *active)
+{
+	NLI_REQUIRE(n >= 1 && n <= kBatchMax, NLI_E_INVALID, "batched updates take 1 to 64 images");
+	cudaStream_t s = ctx->stream;
+	UpdArgs u;
+	fill_upd_args(u, ups[0], 0, 0, C);
+	for (int i = 1; i < n; i++)
+		NLI_REQUIRE(ups[i].patch_x == ups[0].patch_x && ups[i].patch_y == ups[0].patch_y &&
+		                ups[i].sigma == ups[0].sigma,
+		            NLI_E_INVALID, "batched updates share the patch and its sigma");
+	BArgs M, D, P;  // NL-means, NL-medians, NL-Poisson / NL-depth images
+	std::memset(&M, 0, sizeof(M));
+	std::memset(&D, 0, sizeof(D));
+	std::memset(&P, 0, sizeof(P));
+	M.active = D.active = P.active = active;
+	long long maxnh = 0, maxpix = 0;
+	for (int i = 0; i < n; i++) {
+		const UpdBatchItem &it = items[i];
+		const nli_update_params &up = ups[i];
+		NLI_REQUIRE(up.method >= 0 && up.method <= 3, NLI_E_UNSUPPORTED, "unknown update method");
+		if (up.method == NLI_UPDATE_DEPTH) NLI_REQUIRE(C == 4, NLI_E_CHANNELS, "Separate: Channels do not match.");
+		BArgs &B = (up.method == NLI_UPDATE_MEANS) ? M : (up.method == NLI_UPDATE_MEDIANS) ? D : P;
+		BTask &T = B.t[B.n++];
+		T.img_index = it.flag;
+		T.W = it.W;
+		T.H = it.H;
+		T.nh = it.nh;
+		T.img = it.img;
+		T.orig = it.orig;
+		T.dom = it.dom;
+		T.ext = it.ext;
+		T.nnf = reinterpret_cast<const int2 *>(it.nnf);
+		T.conf = it.conf;
+		T.hole = it.hole;
+		T.total = it.total;
+		T.iters = it.cg_iters;
+		maxnh = std::max<long long>(maxnh, it.nh);
+		maxpix = std::max<long long>(maxpix, (long long)it.W * it.H);
+		const size_t np = (size_t)it.W * it.H;
+		const size_t nh = (size_t)std::max(it.nh, 1);
+		if (&B != &P) {
+			const int per = (&B == &M) ? 256 : kMedWarps;
+			T.nparts = div_up(it.nh, per);
+			T.newval = ctx->buf<float>(lk_name(it.flag, "newval"), nh * C);
+			T.partials = ctx->buf<double>(lk_name(it.flag, "partials"), (size_t)std::max(T.nparts, 1));
+			continue;
+		}
+		PoissonArgs &pa = T.pa;
+		pa.W = it.W;
+		pa.H = it.H;
+		pa.C = C;
+		pa.nh = it.nh;
+		for (int c = 0; c < 4; c++) pa.lambda[c] = up.lambda;
+		if (up.method == NLI_UPDATE_DEPTH) pa.lambda[3] = up.lambda_d;
+		pa.tol = up.cg_tol;
+		pa.limit = up.cg_iters;
+		T.hidx = ctx->buf<int32_t>(lk_name(it.flag, "hidx"), np);
+		T.grad = ctx->buf<float>(lk_name(it.flag, "grad"), np * 2 * C);
+		T.co.S = ctx->buf<float>(lk_name(it.flag, "S"), np);
+		T.co.U = ctx->buf<float>(lk_name(it.flag, "U"), np * C);
+		T.co.GX = ctx->buf<float>(lk_name(it.flag, "GX"), np * C);
+		T.co.GY = ctx->buf<float>(lk_name(it.flag, "GY"), np * C);
+		T.unk = ctx->buf<Unknown>(lk_name(it.flag, "unk"), nh);
+		T.b = ctx->buf<float>(lk_name(it.flag, "b"), nh * C);
+		T.x = ctx->buf<float>(lk_name(it.flag, "x"), nh * C);
+		cg_layout(ctx, it.nh, &T.ncta, &T.chunk);
+		if (it.nh == 0) {
+			T.nparts = 0;  // nothing to solve: the step's sum is 0
+		} else if (T.ncta > 0) {
+			T.unkc = ctx->buf<UnkC>(lk_name(it.flag, "unkc"), nh);
+			T.nparts = C * T.ncta;
+		} else {
+			T.nparts = grid_cg_blocks(ctx, it.nh);
+		}
+		T.diff = ctx->buf<double>(lk_name(it.flag, "diff"), (size_t)T.nparts + 1);
+	}
+	const int blk = 256;
+	// ---- NL-means
+	if (M.n > 0) {
+		for (int t = 0; t < M.n; t++) M.blk[t + 1] = M.blk[t] + div_up(M.t[t].nh, 256);
+		if (M.blk[M.n] > 0) {
+			ProfScope ps(ctx, "nlmeans");
+			k_nlmeans_batch<<<M.blk[M.n], 256, 0, s>>>(u, M, C);
+			NLI_CHECK_LAUNCH();
+		}
+		k_scatter_batch<<<per_image_grid(maxnh * C, M.n), blk, 0, s>>>(M, C);
+		NLI_CHECK_LAUNCH();
+		k_total_batch<<<M.n, 1024, 0, s>>>(M, 0);
+		NLI_CHECK_LAUNCH();
+	}
+	// ---- NL-medians
+	if (D.n > 0) {
+		for (int t = 0; t < D.n; t++) D.blk[t + 1] = D.blk[t] + div_up(D.t[t].nh, kMedWarps);
+		if (D.blk[D.n] > 0) {
+			ProfScope ps(ctx, "nlmedians");
+			k_nlmedians_batch<<<D.blk[D.n], 32 * kMedWarps, 0, s>>>(u, D, C);
+			NLI_CHECK_LAUNCH();
+		}
+		k_scatter_batch<<<per_image_grid(maxnh * C, D.n), blk, 0, s>>>(D, C);
+		NLI_CHECK_LAUNCH();
+		k_total_batch<<<D.n, 1024, 0, s>>>(D, 0);
+		NLI_CHECK_LAUNCH();
+	}
+	if (P.n == 0) return;
+	// ---- NL-Poisson / NL-depth: system set-up for every image
+	k_hidx_fill_batch<<<per_image_grid(maxpix, P.n), blk, 0, s>>>(P);
+	NLI_CHECK_LAUNCH();
+	k_hidx_set_batch<<<per_image_grid(maxnh, P.n), blk, 0, s>>>(P);
+	NLI_CHECK_LAUNCH();
+	k_gradient_batch<<<per_image_grid(maxpix * C, P.n), blk, 0, s>>>(P, C);
+	NLI_CHECK_LAUNCH();
+	{
+		ProfScope ps(ctx, "poisson_coef");
+		if (u.px % 2 == 1 && u.py % 2 == 1) {
+			for (int t = 0; t < P.n; t++) P.blk[t + 1] = P.blk[t] + div_up(3LL * P.t[t].nh * 8, 256);
+			if (P.blk[P.n] > 0) k_coef8_batch<<<P.blk[P.n], 256, 0, s>>>(u, P, C);
+		} else {
+			for (int t = 0; t < P.n; t++) P.blk[t + 1] = P.blk[t] + div_up(P.t[t].nh, 128);
+			if (P.blk[P.n] > 0) k_coef_batch<<<P.blk[P.n], 128, 0, s>>>(u, P, C);
+		}
+		if (P.blk[P.n] > 0) NLI_CHECK_LAUNCH();
+	}
+	{
+		ProfScope ps(ctx, "poisson_setup");
+		for (int t = 0; t < P.n; t++) P.blk[t + 1] = P.blk[t] + div_up(P.t[t].nh, 256);
+		if (P.blk[P.n] > 0) {
+			k_setup_batch<<<P.blk[P.n], 256, 0, s>>>(P);
+			NLI_CHECK_LAUNCH();
+		}
+	}
+	k_compact_batch<<<per_image_grid(maxnh, P.n), blk, 0, s>>>(P);
+	NLI_CHECK_LAUNCH();
+	// ---- the solves, one launch per CTA layout
+	const bool pre = ctx->tune_cg_precond != 0;
+	{
+		static std::atomic<uint32_t> raised{0};  // one bit per device
+		const uint32_t bit = 1u << (ctx->device & 31);
+		if (!(raised.load(std::memory_order_acquire) & bit)) {
+			for (int pr = 0; pr < 2; pr++)
+				for (int sg = 0; sg < 2; sg++) {
+					NLI_CUDA(cudaFuncSetAttribute(cg_batch_kernel(pr, sg), cudaFuncAttributeMaxDynamicSharedMemorySize,
+					                              (int)kSmemBudget));
+					if (!sg)
+						NLI_CUDA(cudaFuncSetAttribute(cg_batch_kernel(pr, sg),
+						                              cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+				}
+			raised.fetch_or(bit, std::memory_order_release);
+		}
+	}
+	for (int ncta = 1; ncta <= kClusterMax; ncta++) {
+		CgArgs G;
+		std::memset(&G, 0, sizeof(G));
+		G.C = C;
+		G.ncta = ncta;
+		G.active = active;
+		int maxchunk = 0;
+		for (int t = 0; t < P.n; t++) {
+			const BTask &T = P.t[t];
+			if (T.ncta != ncta || T.nh == 0) continue;
+			CgTask &g = G.t[G.n++];
+			g.img_index = T.img_index;
+			g.a = T.pa;
+			g.chunk = T.chunk;
+			g.unk = T.unkc;
+			g.b = T.b;
+			g.x0 = T.x;
+			g.iters = T.iters;
+			g.hole = T.hole;
+			g.orig = T.orig;
+			g.img = T.img;
+			g.diff = T.diff;
+			maxchunk = std::max(maxchunk, T.chunk);
+		}
+		if (G.n == 0) continue;
+		const size_t smem = (size_t)cluster_vectors(pre) * maxchunk * sizeof(float) + maxchunk * sizeof(UnkC);
+		ProfScope ps(ctx, "poisson_cg");
+		if (ncta == 1) {
+			cg_batch_kernel(pre, true)<<<G.n * C, kClusterBlock, smem, s>>>(G);
+			NLI_CHECK_LAUNCH();
+			continue;
+		}
+		cudaLaunchConfig_t cfg = {};
+		cfg.gridDim = dim3(G.n * C * ncta);
+		cfg.blockDim = dim3(kClusterBlock);
+		cfg.dynamicSmemBytes = smem;
+		cfg.stream = s;
+		cudaLaunchAttribute attr[1];
+		attr[0].id = cudaLaunchAttributeClusterDimension;
+		attr[0].val.clusterDim.x = ncta;
+		attr[0].val.clusterDim.y = 1;
+		attr[0].val.clusterDim.z = 1;
+		cfg.attrs = attr;
+		cfg.numAttrs = 1;
+		NLI_CUDA(cudaLaunchKernelEx(&cfg, cg_batch_kernel(pre, false), G));
+		nli_count_launch_internal();
+	}
+	// systems too large for a cluster: the cooperative grid CG, one at a time
+	for (int t = 0; t < P.n; t++) {
+		const BTask &T = P.t[t];
+		if (T.ncta != 0 || T.nh == 0) continue;
+		const int i = T.img_index;  // names its scratch
+		const size_t nh = (size_t)T.nh;
+		PoissonSystem S;
+		S.pa = T.pa;
+		S.co = T.co;
+		S.unk = T.unk;
+		S.b = T.b;
+		S.x = T.x;
+		GridCgBufs g;
+		g.r = ctx->buf<float>(lk_name(i, "r"), nh * C);
+		g.d = ctx->buf<float>(lk_name(i, "d"), nh * C);
+		g.q = ctx->buf<float>(lk_name(i, "q"), nh * C);
+		g.z = pre ? ctx->buf<float>(lk_name(i, "z"), nh * C) : nullptr;
+		g.part = ctx->buf<double>(lk_name(i, "part"), (size_t)T.nparts * 16);
+		launch_grid_cg(ctx, S, T.nparts, g, T.iters, T.hole, T.orig, T.img, T.diff,
+		               active ? active + T.img_index : nullptr);
+	}
+	k_total_batch<<<P.n, 1024, 0, s>>>(P, 1);
+	NLI_CHECK_LAUNCH();
 }
 
 // ============================================================== adjoints

@@ -5,10 +5,14 @@ Two libraries:
 * ``oracle/_build/libnlioracle.so`` -- the C++ restatement of the reference
   algorithm in ``oracle/nli_oracle.cpp`` (this repository's own code).  Built
   on every machine, including the GPU machine.
+* ``oracle/_build/libnlioracle_timing.so`` -- the same restatement built with
+  the reference's Release flags, only to time the reference algorithm on the
+  host cores (the CPU baseline).
 * ``oracle/_ref/libnliref.so`` (serial, ``-DMETRICS``) and
   ``oracle/_ref/libnliref_omp.so`` (OpenMP) -- the UNMODIFIED reference
-  sources compiled where they lie under ``/root/reference`` together with
-  ``oracle/ref_driver.cpp``.  Built only when that directory exists.  The
+  sources compiled where they lie (``NLI_REFERENCE_DIR``, by default
+  ``/root/reference``) together with ``oracle/ref_driver.cpp``.  Built only
+  when that directory holds them.  The
   reference's own CMake build cannot run here (CMake 4 rejects its minimum
   version and its iio.h forces libpng/libjpeg/libtiff, which are absent), so
   this recipe compiles the sources directly with the flags of the reference's
@@ -24,7 +28,9 @@ from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(HERE)
-REFERENCE = "/root/reference"
+# Where the reference sources lie: NLI_REFERENCE_DIR, else the development
+# container's mount; the reference build is skipped where neither holds them.
+REFERENCE = os.environ.get("NLI_REFERENCE_DIR", "/root/reference")
 REF_OUT = os.path.join(HERE, "_ref")
 BUILD_OUT = os.path.join(HERE, "_build")
 
@@ -67,6 +73,30 @@ def build_oracle(force=False):
         return out
     _run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-fopenmp", *FP_FLAGS,
           "-I", os.path.join(REPO, "include"), src, "-o", out + ".tmp", "-lm"])
+    os.replace(out + ".tmp", out)
+    return out
+
+
+# The flags of the reference's own Release build (CMakeLists.txt: Release
+# -O3 -DNDEBUG, OpenMP compile flags on the target, the compiler's default
+# floating-point contraction), for timing the reference algorithm on the
+# host cores.  Not bit-exact with the reference's float/double rounding on
+# hosts whose compiler contracts multiply-adds (aarch64), so never used as
+# the parity checker.
+TIMING_FLAGS = ["-O3", "-DNDEBUG", "-std=gnu++17", "-fopenmp"]
+
+
+def build_timing(force=False):
+    """Compile the restatement with the reference's Release flags; returns
+    the path of libnlioracle_timing.so."""
+    os.makedirs(BUILD_OUT, exist_ok=True)
+    out = os.path.join(BUILD_OUT, "libnlioracle_timing.so")
+    src = os.path.join(HERE, "nli_oracle.cpp")
+    deps = [src, os.path.join(REPO, "include", "nli.h"), __file__]
+    if not force and _newer(out, deps):
+        return out
+    _run(["g++", *TIMING_FLAGS, "-fPIC", "-shared", "-I", os.path.join(REPO, "include"), src,
+          "-o", out + ".tmp", "-lm"])
     os.replace(out + ".tmp", out)
     return out
 
@@ -117,4 +147,5 @@ def build_reference(force=False):
 if __name__ == "__main__":
     force = "--force" in sys.argv
     print(build_oracle(force))
+    print(build_timing(force))
     print(build_reference(force))

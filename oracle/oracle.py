@@ -228,14 +228,16 @@ class Oracle(_Lib):
     prefix = "orc_"
     parallel_arg = True
 
-    def __init__(self, path=None):
+    def __init__(self, path=None, timing=False):
+        """timing: the build with the reference's Release flags (for timing
+        only; the default build is the bit-exact checker)."""
         if path is None:
             sys.path.insert(0, HERE)
             try:
                 import build as ob
             finally:
                 sys.path.pop(0)
-            path = ob.build_oracle()
+            path = ob.build_timing() if timing else ob.build_oracle()
         super().__init__(path)
         self._energy = self.lib.orc_nnf_energy
         self._energy.restype = I

@@ -1,0 +1,67 @@
+"""The uneven 64-image batch (seed 5, sides log-uniform 128-1024, mixed
+NL-means / NL-Poisson, automatic coarsest rate) against the reference's
+outputs for a fixed subset of its items (tests/golden/batch_reference_*.npz,
+made by tests/golden/make_golden.py --batch: the pinned restatement with the
+reference's OpenMP PatchMatch, seeded).  Image i of a batch with seed s runs
+as a plain process() with seed nli_batch_seed(s, i) -- the lockstep batch
+equals that bit for bit (test_gpu_lockstep.py) -- so each subset item is run
+on its own here.
+
+Contract (the metric's): the hole PSNR of our output against the truth may
+not fall more than 0.1 dB below the reference's, per image."""
+import glob
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+MAX_GAP_DB = 0.1
+BATCH_SEED = 2024  # the seed of the batch comparison in bench.py
+
+
+def hole_psnr(a, truth):
+    d = a.astype(np.float64) - truth.astype(np.float64)
+    return 10 * np.log10(255.0 ** 2 / float(np.mean(d * d)))
+
+
+@pytest.fixture(scope="module")
+def batch_items():
+    from nli_gb300 import workloads as wl
+    return wl.config5(seed=5, count=64, max_side=1024)
+
+
+def golden_files():
+    return sorted(glob.glob(os.path.join(GOLDEN, "batch_reference_*.npz")))
+
+
+def test_subset_covers_the_size_range():
+    sizes = []
+    for path in golden_files():
+        g = np.load(path)
+        assert tuple(g["batch"]) == (5, 64, 1024)
+        sizes.append(int(g["index"]))
+    assert len(sizes) >= 8
+
+
+@pytest.mark.parametrize("path", golden_files(), ids=lambda p: os.path.basename(p)[:-4])
+def test_batch_item_vs_reference(gpu_ctx, batch_items, path):
+    from nli_gb300 import workloads as wl
+    g = np.load(path)
+    i = int(g["index"])
+    img, mask, method, scales = batch_items[i]
+    p = wl.config5_params(mask, method, scales)
+    gpu_ctx.set_seed(gpu_ctx.batch_seed(BATCH_SEED, i))
+    out, st = gpu_ctx.process(img, mask, p)
+    hole = mask > 0
+    truth = img[hole]
+    ours, ref = hole_psnr(out[hole], truth), hole_psnr(g["hole"], truth)
+    print(json.dumps({"index": i, "size": [img.shape[1], img.shape[0]], "method": method, "scales": p.scales,
+                      "psnr_ours_db": ours, "psnr_reference_db": ref, "gap_db": ours - ref,
+                      "iterations": st["iterations"]}))
+    assert np.array_equal(out[~hole], img[~hole])
+    assert ref - ours <= MAX_GAP_DB, (i, ours, ref)

@@ -117,7 +117,7 @@ def test_cli_matches_c_abi(cli, gpu_ctx, tmp_path):
                        cwd=tmp_path, capture_output=True, text=True)
     print(r.stdout, r.stderr)
     assert r.returncode == 0, r.stderr
-    name = "out_nlmeans_sc3_0.5_initnone_ps9_10000_conf5_0.1.png"  # main.cpp's composed name
+    name = "out_nlmeans_sc3_0.5_initpoisson_ps9_10000_conf5_0.1.png"  # main.cpp's composed name, with Poisson initialisation named as such
     assert name in r.stdout
     got = read_png(tmp_path / name)
     # the same steps through the C ABI: Lab, process with the CLI's pairing
@@ -158,7 +158,7 @@ def test_cli_png_inputs_and_channel_rules(cli, gpu_ctx, tmp_path):
                         "-coarse", "0.5", "-iters", "8", "-seed", "3"], cwd=tmp_path, capture_output=True, text=True)
     print(r.stdout, r.stderr)
     assert r.returncode == 0, r.stderr
-    got = read_png(tmp_path / "out_nlmeans_sc3_0.5_initnone_ps9_10000_conf5_0.1.png")
+    got = read_png(tmp_path / "out_nlmeans_sc3_0.5_initpoisson_ps9_10000_conf5_0.1.png")
     rgb = np.stack([grey, alpha, grey], -1).astype(np.float32)
     p = wl.params("nlmeans", distance="l2", patch=9, scales=3, coarse=0.5, iters=8)
     p.patchmatch.random_shots = 30

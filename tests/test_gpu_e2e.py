@@ -1,13 +1,15 @@
 """End-to-end on the full-size benchmark configurations (1: 256x256 nlmeans,
 2: 512x512 nlpoisson, 3: 640x480 nldepth), against the reference's own
-output for the same input (tests/golden/config*_reference.npz, produced by
-the serial reference build with srand(101)).
+output for the same inputs: three input seeds per configuration
+(tests/golden/config*_reference*.npz, produced by the serial reference build
+with srand(101) by tests/golden/make_golden.py --full --seeds).
 
 The GPU PatchMatch draws different random numbers and sweeps in parallel,
-so the inpainting reaches a different (similar) solution: the comparison
-is the hole-region PSNR of the GPU output against the reference output, and
-the gap between the reference's and the GPU's hole PSNR against the ground
-truth (the synthetic image before masking)."""
+so the inpainting reaches a different (similar) solution.  The contract is
+the metric's: the hole-region PSNR of the GPU output against the ground
+truth (the synthetic image before masking) may not fall more than 0.1 dB
+below the reference's, as the mean over the seeds, per channel group.  The
+per-seed figures are printed."""
 import json
 import os
 
@@ -18,20 +20,28 @@ from conftest import GOLDEN
 
 pytestmark = pytest.mark.gpu
 
+SEEDS = (0, 1, 2)
+MAX_GAP_DB = 0.1  # reference PSNR minus ours, mean over the seeds
+
 
 def psnr(a, b, peak):
     mse = float(np.mean((a.astype(np.float64) - b.astype(np.float64)) ** 2))
     return float("inf") if mse == 0 else 10 * np.log10(peak * peak / mse)
 
 
-@pytest.mark.parametrize("name", ["config1", "config2", "config3"])
-def test_full_size_vs_reference(gpu_ctx, name):
+def reference_path(name, seed):
+    return os.path.join(GOLDEN, "%s_reference.npz" % name if seed == 0 else "%s_reference_seed%d.npz" % (name, seed))
+
+
+def run_seed(gpu_ctx, name, seed):
     from nli_gb300 import workloads as wl
-    g = np.load(os.path.join(GOLDEN, "%s_reference.npz" % name))
-    img, mask, p = getattr(wl, name)(seed=0)
+    g = np.load(reference_path(name, seed))
+    img, mask, p = getattr(wl, name)(seed=seed)
     gpu_ctx.set_seed(101)
     out, st = gpu_ctx.process(img, mask, p)
     hole = mask > 0
+    assert np.isfinite(out).all()
+    assert np.array_equal(out[~hole], img[~hole])
     ref_hole = g["hole"]
     rows = []
     # colour channels on a 0-255 peak; the depth channel of configuration 3
@@ -41,14 +51,28 @@ def test_full_size_vs_reference(gpu_ctx, name):
         chans.append((slice(3, 4), float(img[..., 3].max() - img[..., 3].min())))
     for sl, peak in chans:
         o, r, t = out[hole][:, sl], ref_hole[:, sl], img[hole][:, sl]
-        vs_ref = psnr(o, r, peak)
-        gpu_gt, ref_gt = psnr(o, t, peak), psnr(r, t, peak)
-        rows.append({"channels": "%d:%d" % (sl.start, sl.stop), "psnr_gpu_vs_ref": vs_ref,
-                     "psnr_gpu_vs_truth": gpu_gt, "psnr_ref_vs_truth": ref_gt, "gap_db": ref_gt - gpu_gt})
-    report = {"workload": name, "iterations_gpu": st["iterations"], "rows": rows}
-    print(json.dumps(report))
-    assert np.isfinite(out).all()
-    assert np.array_equal(out[~hole], img[~hole])
+        rows.append({"seed": seed, "channels": "%d:%d" % (sl.start, sl.stop), "psnr_gpu_vs_ref": psnr(o, r, peak),
+                     "psnr_gpu_vs_truth": psnr(o, t, peak), "psnr_ref_vs_truth": psnr(r, t, peak)})
+    return rows, st
+
+
+@pytest.mark.parametrize("name", ["config1", "config2", "config3"])
+def test_full_size_vs_reference(gpu_ctx, name):
+    rows = []
+    for seed in SEEDS:
+        r, st = run_seed(gpu_ctx, name, seed)
+        rows += r
+    groups = sorted({r["channels"] for r in rows})
+    summary = []
+    for ch in groups:
+        sel = [r for r in rows if r["channels"] == ch]
+        gpu = float(np.mean([r["psnr_gpu_vs_truth"] for r in sel]))
+        ref = float(np.mean([r["psnr_ref_vs_truth"] for r in sel]))
+        summary.append({"channels": ch, "mean_psnr_gpu_vs_truth": gpu, "mean_psnr_ref_vs_truth": ref,
+                        "mean_gap_db": ref - gpu})
+    print(json.dumps({"workload": name, "seeds": list(SEEDS), "rows": rows, "summary": summary}))
     for r in rows:
+        # a sanity bound per seed: the two outputs are the same kind of fill
         assert r["psnr_gpu_vs_ref"] > 15.0, r
-        assert r["gap_db"] < 3.0, r
+    for s in summary:
+        assert s["mean_gap_db"] <= MAX_GAP_DB, s

@@ -87,27 +87,36 @@ def test_graph_stops_on_tolerance_and_limit(gpu_ctx):
             assert all(i == iters for i in a[1]["iterations"][:2])
 
 
-def test_graph_batch_equals_host_loop(gpu_ctx):
-    """Batches take the graph only with NLI_TUNE_GRAPH_LOOP = 2 (1 keeps their
-    host loop); outputs are identical either way."""
+@pytest.mark.parametrize("mode", [0, 1])
+def test_graph_batch_equals_host_loop(gpu_ctx, mode):
+    """Lockstep batches (NLI_TUNE_BATCH_MODE 1) run each rank's iterations in
+    a graph whenever the graph loop is on; the worker-context form (0) only
+    with NLI_TUNE_GRAPH_LOOP = 2 (1 keeps its host loop).  Outputs are
+    identical either way."""
     from test_gpu_batch import small_batch
     items, params = small_batch(count=5, seed=21)
-    gpu_ctx.set_seed(9)
-    gpu_ctx.set_tuning(gpu_ctx.TUNE_GRAPH_LOOP, 1)
-    outs_1, st_1 = gpu_ctx.process_batch(items, params)
-    assert all(s["graph_iterations"] == 0 for s in st_1)
-    gpu_ctx.set_seed(9)
-    gpu_ctx.set_tuning(gpu_ctx.TUNE_GRAPH_LOOP, 2)
-    outs_g, st_g = gpu_ctx.process_batch(items, params)
-    assert all(s["graph_iterations"] > 0 for s in st_g)
-    for a, b in zip(outs_g, outs_1):
-        assert np.array_equal(a, b)
-    gpu_ctx.set_tuning(gpu_ctx.TUNE_GRAPH_LOOP, 0)
+    gpu_ctx.set_tuning(gpu_ctx.TUNE_BATCH_MODE, mode)
     try:
         gpu_ctx.set_seed(9)
-        outs_h, _ = gpu_ctx.process_batch(items, params)
+        gpu_ctx.set_tuning(gpu_ctx.TUNE_GRAPH_LOOP, 1)
+        outs_1, st_1 = gpu_ctx.process_batch(items, params)
+        if mode == 0:
+            assert all(s["graph_iterations"] == 0 for s in st_1)
+        else:
+            assert all(s["graph_iterations"] > 0 for s in st_1)
+        gpu_ctx.set_seed(9)
+        gpu_ctx.set_tuning(gpu_ctx.TUNE_GRAPH_LOOP, 2)
+        outs_g, st_g = gpu_ctx.process_batch(items, params)
+        assert all(s["graph_iterations"] > 0 for s in st_g)
+        for a, b in zip(outs_g, outs_1):
+            assert np.array_equal(a, b)
+        gpu_ctx.set_tuning(gpu_ctx.TUNE_GRAPH_LOOP, 0)
+        gpu_ctx.set_seed(9)
+        outs_h, st_h = gpu_ctx.process_batch(items, params)
+        assert all(s["graph_iterations"] == 0 for s in st_h)
     finally:
         gpu_ctx.set_tuning(gpu_ctx.TUNE_GRAPH_LOOP, 1)
+        gpu_ctx.set_tuning(gpu_ctx.TUNE_BATCH_MODE, 1)
     for a, b in zip(outs_g, outs_h):
         assert np.array_equal(a, b)
 

@@ -18,7 +18,7 @@ class FakeCtx:
     def __init__(self):
         import nli_gb300 as pkg
         for k in ("TUNE_CG_CLUSTER_CAP", "TUNE_CG_UNKNOWNS_PER_CTA", "TUNE_BATCH_WIDTH", "TUNE_PM_VARIANT",
-                  "TUNE_CG_PRECOND", "TUNE_GRAPH_LOOP"):
+                  "TUNE_CG_PRECOND", "TUNE_GRAPH_LOOP", "TUNE_CG_SINGLE_MAX", "TUNE_BATCH_MODE"):
             setattr(self, k, getattr(pkg.Context, k))
         self.tuning = {}
         self.batch_width = None
@@ -53,7 +53,7 @@ def test_tuning_constants_match_the_header():
     here = os.path.dirname(os.path.abspath(__file__))
     header = open(os.path.join(here, "..", "include", "nli.h")).read()
     defines = dict((m.group(1), int(m.group(2))) for m in re.finditer(r"#define NLI_(TUNE_\w+) (\d+)", header))
-    assert len(defines) == 6
+    assert len(defines) == 8
     for name, value in defines.items():
         assert getattr(pkg.Context, name) == value, name
 
