@@ -181,6 +181,24 @@ def cpu_sample(img, mask, p, iterations):
     return est, wall, orc.max_threads
 
 
+def formula_candidates(st, pm_iterations=10):
+    """The candidates the reference's PatchMatch evaluates in one process()
+    by the hot-path formula: per call N_t (1 + I (2 + W_rs)), with N_t the
+    scale's target points, I the sweeps and W_rs = floor(log2 max(W, H)) + 1
+    random-search windows; calls per scale = its iterations plus one per
+    scale transition it takes part in (propagate_weights runs PatchMatch on
+    the coarser and on the finer scale)."""
+    import math
+    S = st["scales"]
+    total = 0
+    for l in range(S):
+        W, H, nt = st["width"][l], st["height"][l], st["targets"][l]
+        windows = int(math.floor(math.log2(max(W, H)))) + 1
+        calls = st["iterations"][l] + (1 if l < S - 1 else 0) + (1 if l > 0 else 0)
+        total += calls * nt * (1 + pm_iterations * (2 + windows))
+    return total
+
+
 def cpu_calibration():
     """Checks the per-scale sampling of cpu_sample against a whole timed
     process() on the 256x256 NL-means workload: the OpenMP restatement (the
@@ -393,14 +411,26 @@ def run_ours(args):
         import re
         m = re.search(r"traffic_bytes_per_launch:\s*(\d+)", open(TRAFFIC).read())
         traffic = int(m.group(1)) if m else None
-    pm_tflops = cand * flop_per_candidate() / (pm_ms / 1e3) / 1e12 if pm_ms > 0 else 0.0
+    stats = st.as_dict()
+    formula = formula_candidates(stats, p.patchmatch.iterations) * args.steps
+    pm_tflops = formula * flop_per_candidate() / (pm_ms / 1e3) / 1e12 if pm_ms > 0 else 0.0
+    eval_tflops = cand * flop_per_candidate() / (pm_ms / 1e3) / 1e12 if pm_ms > 0 else 0.0
     roofline = {"kernel": "k_pm_init + k_pm_sweep (PatchMatch)", "bound": "fp32", "achieved": pm_tflops,
                 "peak": fp32_peak, "unit": "TFLOP/s", "frac": pm_tflops / fp32_peak if fp32_peak else None,
                 "traffic": traffic, "traffic_scope": "ncu DRAM bytes of one finest-scale (512x512) sweep launch",
                 "launches": pm_launches, "ms": pm_ms,
                 "peak_source": "nominal FP32 (%d SMs x 128 lanes x 2 FLOP) at the sampled median SM clock %.0f MHz; "
                                "MEASURED_PEAKS.json has no FP32 figure" % (n_sm, sm_mhz),
-                "flop_per_candidate": flop_per_candidate(), "candidates": cand}
+                "flop_per_candidate": flop_per_candidate(),
+                "work": "algorithmic: the reference's candidates by the hot-path formula, per PatchMatch call "
+                        "N_t (1 + I (2 + W_rs)), summed over the run's calls",
+                "formula_candidates": formula,
+                "evaluated_candidates": cand,
+                "evaluated_tflops": eval_tflops,
+                "evaluated_note": "candidates the kernels evaluated (the patch-mean lower bound skips the rest), "
+                                  "each counted at the full 2519 FLOP though %.1f %% of them stopped after 4 of "
+                                  "10 rows" % (100.0 * (c1["candidates_partial"] - c0["candidates_partial"])
+                                                / max(cand, 1))}
     cg = prof.get("poisson_cg", (0, 0.0))
     cg_work = c1["cg_unknown_iterations"] - c0["cg_unknown_iterations"]
     cg_gbs = cg_work * CG_BYTES_PER_UNKNOWN_ITER / (cg[1] / 1e3) / 1e9 if cg[1] > 0 else 0.0
@@ -534,6 +564,19 @@ def batch_compare(pkg, ctx, args, local):
     launches = ctx.launch_count() - l0
     tp = timed(plain)
     identical = all(bool(torch.equal(x, y)) for x, y in zip(outs, ref))
+    by_groups = None
+    if args.batch_groups_sweep:
+        # the lockstep batch per number of concurrent sub-groups
+        by_groups = {}
+        keep = ctx.get_tuning(ctx.TUNE_BATCH_GROUPS)
+        try:
+            for g in (1, 2, 4):
+                ctx.set_tuning(ctx.TUNE_BATCH_GROUPS, g)
+                batched()
+                by_groups[str(g)] = round(timed(batched), 3)
+                identical = identical and all(bool(torch.equal(x, y)) for x, y in zip(outs, ref))
+        finally:
+            ctx.set_tuning(ctx.TUNE_BATCH_GROUPS, keep)
     workers = None
     if args.batch_workers:
         batched(0)
@@ -557,9 +600,11 @@ def batch_compare(pkg, ctx, args, local):
                         "holes, nlmeans/nlpoisson alternating, patch 9, scales |round(log(0.1 size)/log(0.75))|, "
                         "automatic coarsest rate (seed 5)" % (len(items), args.batch_max_side),
             "mpix": mpix, "plain_mpix_s": mpix / tp, "batched_mpix_s": mpix / tb, "speedup": tp / tb,
-            "plain_s": tp, "batched_s": tb,
+            "plain_s": tp, "batched_s": tb, "batch_groups": ctx.get_tuning(ctx.TUNE_BATCH_GROUPS),
+            "batched_s_by_groups": by_groups,
             "batched_path": "lockstep: one launch per kernel per pyramid rank over every image, each rank's "
-                            "iteration loop one CUDA graph (while node, per-image stopping test on the device)",
+                            "iteration loop one CUDA graph (while node, per-image stopping test on the device); "
+                            "the images dealt into concurrent sub-groups on worker contexts",
             "plain_path": "one process() per image, iterations after a scale's first in one CUDA graph",
             "gpu_launches": int(launches), "identical_to_plain": identical,
             "reference_psnr": gaps,
@@ -583,6 +628,21 @@ def run_case(args):
         ctx.set_tuning(ctx.TUNE_CG_PRECOND, args.cg_precond)
     ctx.set_seed(7)
     img, mask, p = workload()
+    if args.case == "batch":
+        # one lockstep batch of the uneven-batch workload (--batch-count
+        # images, sides up to --batch-max-side), --steps times
+        from nli_gb300 import workloads as wl
+        items5 = wl.config5(seed=5, count=args.batch_count, max_side=args.batch_max_side)
+        items = [(ctx._f32(i), ctx._u8(m)) for i, m, _, _ in items5]
+        params = [wl.config5_params(m, meth, sc) for _, m, meth, sc in items5]
+        l0 = ctx.launch_count()
+        for _ in range(args.steps):
+            ctx.set_seed(2024)
+            ctx.process_batch_device(items, params)
+        torch.cuda.synchronize()
+        print(json.dumps({"case": "batch", "images": len(items), "launches": ctx.launch_count() - l0,
+                          "counters": ctx.counters()}))
+        return 0
     if args.case == "process":
         d_img, d_mask = ctx._f32(img), ctx._u8(mask)
         d_out = torch.empty_like(d_img)
@@ -611,7 +671,7 @@ def run_case(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default=None, choices=["patchmatch", "update", "process"],
+    ap.add_argument("--case", default=None, choices=["patchmatch", "update", "process", "batch"],
                     help="run one small profiling case instead of the benchmark")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -637,6 +697,8 @@ def main():
     ap.add_argument("--batch-profile", action="store_true",
                     help="add per-kernel profiled passes of both paths to the batch comparison")
     ap.add_argument("--no-batch-profile", dest="batch_profile", action="store_false")
+    ap.add_argument("--batch-groups-sweep", action="store_true",
+                    help="also time the lockstep batch with 1, 2 and 4 concurrent sub-groups")
     ap.add_argument("--batch-workers", action="store_true",
                     help="also time the worker-context batch form (NLI_TUNE_BATCH_MODE 0)")
     args = ap.parse_args()

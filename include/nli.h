@@ -131,6 +131,11 @@ typedef struct nli_process_stats {
 	int64_t candidates;                  /* patch distances evaluated by PatchMatch */
 	int64_t graph_iterations;            /* of the iterations, those run in captured loops
 	                                        (NLI_TUNE_GRAPH_LOOP) */
+	int32_t targets[NLI_MAX_SCALES];     /* PatchMatch target points per scale (the
+	                                        extended domain minus the margin) */
+	int32_t holes[NLI_MAX_SCALES];       /* hole pixels per scale (the CG's unknowns) */
+	int64_t candidates_partial;          /* of the candidates, those stopped after the
+	                                        early-termination test */
 } nli_process_stats;
 
 typedef struct nli_ctx nli_ctx;
@@ -438,6 +443,23 @@ int nli_ctx_set_batch_width(nli_ctx *ctx, int width);
  *                                  one CUDA graph; 0 worker contexts -- up to
  *                                  the batch width of whole nli_process runs
  *                                  on their own streams.  Identical results.
+ *   NLI_TUNE_PM_BOUND              1 (default): PatchMatch skips a candidate
+ *                                  whose patch means (of the image and its
+ *                                  forward differences, weighted by the patch
+ *                                  weights) differ from the target's by
+ *                                  enough that, by Jensen's inequality, its
+ *                                  distance cannot beat the current match;
+ *                                  0: every candidate is evaluated.  The
+ *                                  bound keeps a rounding margin, so fields
+ *                                  and distances are identical either way.
+ *   NLI_TUNE_BATCH_GROUPS          lockstep batches: the images of one
+ *                                  launch-sharing group are dealt (largest
+ *                                  first, to the least-loaded) into this many
+ *                                  sub-groups that run concurrently on their
+ *                                  own streams and workspaces, so one
+ *                                  sub-group's per-rank tail (its slowest
+ *                                  image) overlaps another's work (1..16,
+ *                                  default 2).  Identical results.
  * nli_ctx_get_tuning reads them back. */
 #define NLI_TUNE_CG_CLUSTER_CAP 0
 #define NLI_TUNE_CG_UNKNOWNS_PER_CTA 1
@@ -447,6 +469,8 @@ int nli_ctx_set_batch_width(nli_ctx *ctx, int width);
 #define NLI_TUNE_GRAPH_LOOP 5
 #define NLI_TUNE_CG_SINGLE_MAX 6
 #define NLI_TUNE_BATCH_MODE 7
+#define NLI_TUNE_PM_BOUND 8
+#define NLI_TUNE_BATCH_GROUPS 9
 int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value);
 int nli_ctx_get_tuning(nli_ctx *ctx, int knob, int *value);
 /* The seed image `index` of a batch runs with. */

@@ -61,7 +61,9 @@ class ProcessStats(ct.Structure):
                 ("last_difference", ct.c_double * NLI_MAX_SCALES),
                 ("patchmatch_calls", ct.c_int64), ("update_calls", ct.c_int64),
                 ("cg_iterations", ct.c_int64), ("candidates", ct.c_int64),
-                ("graph_iterations", ct.c_int64)]
+                ("graph_iterations", ct.c_int64),
+                ("targets", ct.c_int32 * NLI_MAX_SCALES), ("holes", ct.c_int32 * NLI_MAX_SCALES),
+                ("candidates_partial", ct.c_int64)]
 
     def as_dict(self):
         n = self.scales
@@ -70,7 +72,8 @@ class ProcessStats(ct.Structure):
                 "last_difference": list(self.last_difference[:n]),
                 "patchmatch_calls": self.patchmatch_calls, "update_calls": self.update_calls,
                 "cg_iterations": self.cg_iterations, "candidates": self.candidates,
-                "graph_iterations": self.graph_iterations}
+                "graph_iterations": self.graph_iterations, "targets": list(self.targets[:n]),
+                "holes": list(self.holes[:n]), "candidates_partial": self.candidates_partial}
 
 
 _libm = None

@@ -1,13 +1,16 @@
 """Autotuner for the launch shapes the library leaves open: the size of the
 thread-block clusters of the NL-Poisson conjugate gradient (CTAs per
-cluster, unknowns per CTA), the way the 9x9 PatchMatch kernels read their
-windows (NLI_TUNE_PM_VARIANT) and the number of images a batch keeps in
-flight.  Each candidate is timed with CUDA events on a representative case
-on the context's own device; the fastest is set on the context
+cluster, unknowns per CTA), the largest CG system one CTA solves alone
+(NLI_TUNE_CG_SINGLE_MAX), the way the 9x9 PatchMatch kernels read their
+windows (NLI_TUNE_PM_VARIANT), the PatchMatch lower-bound test
+(NLI_TUNE_PM_BOUND), how a batch runs (NLI_TUNE_BATCH_MODE, the worker
+contexts' width, the lockstep sub-groups NLI_TUNE_BATCH_GROUPS).  Each
+candidate is timed with CUDA events on a representative case on the
+context's own device; the fastest is set on the context
 (nli_ctx_set_tuning) and returned with the whole table, which callers may
 store and re-apply with apply().  Results depend on these shapes only
-through the float rounding of the CG's sums; the PatchMatch variants give
-identical fields.
+through the float rounding of the CG's sums; the PatchMatch variants and
+the bound give identical fields, the batch forms identical images.
 """
 from __future__ import annotations
 
@@ -122,6 +125,105 @@ def tune_batch_width(ctx, items, params, widths=(2, 4, 8, 12, 16)):
     return {"best": choice, "ms": times}
 
 
+def _time_update(ctx, case, repeats):
+    import torch
+    upd, u, mask, ext, nnf, conf = case
+    ctx.update(upd, u, u, mask, ext, nnf, conf)  # warm
+    best = float("inf")
+    for _ in range(repeats):
+        torch.cuda.synchronize()
+        a, b = _events(torch)
+        a.record()
+        ctx.update(upd, u, u, mask, ext, nnf, conf)
+        b.record()
+        torch.cuda.synchronize()
+        best = min(best, a.elapsed_time(b))
+    return best
+
+
+def tune_cg_single(ctx, cases=None, limits=(0, 512, 1024, 2048, 4096), repeats=3):
+    """Times NL-Poisson updates of a few small systems (the coarse pyramid
+    levels' sizes) per one-CTA limit and keeps the limit with the smallest
+    total.  Returns {"best": limit, "ms": {limit: ms}}."""
+    if cases is None:
+        cases = [poisson_case(ctx, size=s, seed=1) for s in (48, 72, 96, 128)]
+    times = {}
+    for lim in limits:
+        ctx.set_tuning(ctx.TUNE_CG_SINGLE_MAX, lim)
+        times[lim] = sum(_time_update(ctx, c, repeats) for c in cases)
+    choice = min(times, key=times.get)
+    ctx.set_tuning(ctx.TUNE_CG_SINGLE_MAX, choice)
+    return {"best": choice, "ms": times}
+
+
+def tune_pm_bound(ctx, case=None, repeats=3, seed=0):
+    """Times one PatchMatch call with and without the lower-bound test and
+    keeps the faster.  Returns {"best": 0 or 1, "ms": {0: ms, 1: ms}}."""
+    import torch
+    dist, pm, u, src, tgt = case if case is not None else patchmatch_case(ctx)
+    times = {}
+    for v in (0, 1):
+        ctx.set_tuning(ctx.TUNE_PM_BOUND, v)
+        ctx.set_seed(seed)
+        ctx.patchmatch(dist, pm, u, src, u, tgt, want_energy=False)  # warm
+        best = float("inf")
+        for _ in range(repeats):
+            ctx.set_seed(seed)
+            torch.cuda.synchronize()
+            a, b = _events(torch)
+            a.record()
+            ctx.patchmatch(dist, pm, u, src, u, tgt, want_energy=False)
+            b.record()
+            torch.cuda.synchronize()
+            best = min(best, a.elapsed_time(b))
+        times[v] = best
+    choice = min(times, key=times.get)
+    ctx.set_tuning(ctx.TUNE_PM_BOUND, choice)
+    return {"best": choice, "ms": times}
+
+
+def _time_batch(ctx, items, params):
+    import torch
+    torch.cuda.synchronize()
+    a, b = _events(torch)
+    a.record()
+    ctx.process_batch_device(items, params)
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b)
+
+
+def tune_batch_mode(ctx, items, params):
+    """Times process_batch_device on device-resident `items` in the lockstep
+    form (1) and the worker-context form (0) and keeps the faster.  Returns
+    {"best": mode, "ms": {mode: ms}}."""
+    times = {}
+    for mode in (1, 0):
+        ctx.set_tuning(ctx.TUNE_BATCH_MODE, mode)
+        times[mode] = _time_batch(ctx, items, params)
+    choice = min(times, key=times.get)
+    ctx.set_tuning(ctx.TUNE_BATCH_MODE, choice)
+    return {"best": choice, "ms": times}
+
+
+def tune_batch_groups(ctx, items, params, groups=(1, 2, 4)):
+    """Times lockstep process_batch_device on device-resident `items` per
+    number of concurrent sub-groups and keeps the fastest.  Returns
+    {"best": groups, "ms": {groups: ms}}."""
+    mode = ctx.get_tuning(ctx.TUNE_BATCH_MODE)
+    ctx.set_tuning(ctx.TUNE_BATCH_MODE, 1)
+    times = {}
+    try:
+        for g in groups:
+            ctx.set_tuning(ctx.TUNE_BATCH_GROUPS, g)
+            times[g] = _time_batch(ctx, items, params)
+    finally:
+        ctx.set_tuning(ctx.TUNE_BATCH_MODE, mode)
+    choice = min(times, key=times.get)
+    ctx.set_tuning(ctx.TUNE_BATCH_GROUPS, choice)
+    return {"best": choice, "ms": times}
+
+
 def device_key(device=0):
     """The cache key of a device: its name, SM count and compute capability."""
     import torch
@@ -129,7 +231,11 @@ def device_key(device=0):
     return "%s|%d SMs|sm_%d%d" % (pr.name, pr.multi_processor_count, pr.major, pr.minor)
 
 
-def save(path, key, cg=None, batch_width=None, pm_variant=None):
+_SCALARS = ("batch_width", "pm_variant", "cg_single", "pm_bound", "batch_mode", "batch_groups")
+
+
+def save(path, key, cg=None, batch_width=None, pm_variant=None, cg_single=None, pm_bound=None, batch_mode=None,
+         batch_groups=None):
     """Stores the choices for one device key in a JSON cache file (other
     devices' entries are kept)."""
     import json
@@ -141,10 +247,11 @@ def save(path, key, cg=None, batch_width=None, pm_variant=None):
     entry = {}
     if cg is not None:
         entry["cg"] = [int(cg[0]), int(cg[1])]
-    if batch_width is not None:
-        entry["batch_width"] = int(batch_width)
-    if pm_variant is not None:
-        entry["pm_variant"] = int(pm_variant)
+    values = dict(batch_width=batch_width, pm_variant=pm_variant, cg_single=cg_single, pm_bound=pm_bound,
+                  batch_mode=batch_mode, batch_groups=batch_groups)
+    for name in _SCALARS:
+        if values[name] is not None:
+            entry[name] = int(values[name])
     table[key] = entry
     tmp = path + ".tmp"
     with open(tmp, "w") as f:
@@ -163,16 +270,20 @@ def load(ctx, path, key):
         entry = json.load(f).get(key)
     if entry is None:
         return None
-    apply(ctx, cg=entry.get("cg"), batch_width=entry.get("batch_width"), pm_variant=entry.get("pm_variant"))
+    apply(ctx, cg=entry.get("cg"), **{name: entry.get(name) for name in _SCALARS})
     return entry
 
 
-def apply(ctx, cg=None, batch_width=None, pm_variant=None):
+def apply(ctx, cg=None, batch_width=None, pm_variant=None, cg_single=None, pm_bound=None, batch_mode=None,
+          batch_groups=None):
     """Re-applies stored choices: cg = (cap, unknowns per CTA)."""
     if cg is not None:
         ctx.set_tuning(ctx.TUNE_CG_CLUSTER_CAP, int(cg[0]))
         ctx.set_tuning(ctx.TUNE_CG_UNKNOWNS_PER_CTA, int(cg[1]))
-    if pm_variant is not None:
-        ctx.set_tuning(ctx.TUNE_PM_VARIANT, int(pm_variant))
+    for knob, value in ((ctx.TUNE_PM_VARIANT, pm_variant), (ctx.TUNE_CG_SINGLE_MAX, cg_single),
+                        (ctx.TUNE_PM_BOUND, pm_bound), (ctx.TUNE_BATCH_MODE, batch_mode),
+                        (ctx.TUNE_BATCH_GROUPS, batch_groups)):
+        if value is not None:
+            ctx.set_tuning(knob, int(value))
     if batch_width is not None:
         ctx.set_batch_width(int(batch_width))

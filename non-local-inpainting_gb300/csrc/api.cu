@@ -654,6 +654,14 @@ int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value)
 		if (value != 0 && value != 1) return NLI_E_INVALID;
 		ctx->tune_batch_mode = value;
 		return NLI_OK;
+	case NLI_TUNE_PM_BOUND:
+		if (value != 0 && value != 1) return NLI_E_INVALID;
+		ctx->tune_pm_bound = value;
+		return NLI_OK;
+	case NLI_TUNE_BATCH_GROUPS:
+		if (value < 1 || value > 16) return NLI_E_INVALID;
+		ctx->tune_batch_groups = value;
+		return NLI_OK;
 	}
 	return NLI_E_INVALID;
 }
@@ -670,6 +678,8 @@ int nli_ctx_get_tuning(nli_ctx *ctx, int knob, int *value)
 	case NLI_TUNE_GRAPH_LOOP: *value = ctx->tune_graph_loop; return NLI_OK;
 	case NLI_TUNE_CG_SINGLE_MAX: *value = ctx->tune_cg_single_max; return NLI_OK;
 	case NLI_TUNE_BATCH_MODE: *value = ctx->tune_batch_mode; return NLI_OK;
+	case NLI_TUNE_PM_BOUND: *value = ctx->tune_pm_bound; return NLI_OK;
+	case NLI_TUNE_BATCH_GROUPS: *value = ctx->tune_batch_groups; return NLI_OK;
 	}
 	return NLI_E_INVALID;
 }

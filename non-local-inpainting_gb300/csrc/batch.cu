@@ -27,7 +27,7 @@ uint64_t batch_seed(uint64_t seed, int index)
 	return seed ^ (0x9E3779B97F4A7C15ULL * (uint64_t)(index + 1));
 }
 
-static nli_ctx *new_worker(int device)
+nli_ctx *new_worker(int device)
 {
 	nli_ctx *w = nullptr;
 	const int rc = nli_ctx_create(device, &w);
@@ -37,7 +37,7 @@ static nli_ctx *new_worker(int device)
 }
 
 // Adds a worker's profile and counters to the parent and clears them.
-static void merge_worker(nli_ctx *parent, nli_ctx *w)
+void merge_worker(nli_ctx *parent, nli_ctx *w)
 {
 	w->settle_profile();
 	for (auto &kv : w->prof) {

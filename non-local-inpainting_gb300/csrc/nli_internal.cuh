@@ -133,7 +133,9 @@ struct nli_ctx {
 	int tune_graph_loop = 1;             // iterations 1.. of a scale as one CUDA graph (while node):
 	                                     // 1 in nli_process only, 2 also in batches, 0 never
 	int tune_cg_single_max = 1024;       // CG systems of at most this many unknowns: one CTA
-	int tune_batch_mode = 1;             // batches: 1 lockstep (lockstep.cu), 0 worker contexts (batch.cu)
+	int tune_batch_mode = 1;             // batches: 1 lockstep (process.cu), 0 worker contexts (batch.cu)
+	int tune_pm_bound = 1;               // PatchMatch: skip candidates by the patch-mean lower bound
+	int tune_batch_groups = 2;           // lockstep: concurrent sub-groups per launch-sharing group
 	bool batch_worker = false;           // a worker context of nli_process_batch
 	int max_smem_optin = 0;              // dynamic shared memory per block at most
 	std::vector<nli_ctx *> workers;
@@ -281,6 +283,8 @@ struct PmBatchItem {
 	unsigned long long *calls;    // the image's PatchMatch call index (device)
 	unsigned long long *counter;  // the image's candidate counters (2, device) or null
 	int flag;                     // index of the image's active flag
+	float4 *mom;                  // (W + 1) * (H + 1) patch means of the lower bound, or null
+	unsigned *vmax;               // the image's largest absolute value (float bits), with mom
 };
 // active: device flags (null: all), item i reads active[items[i].flag];
 // inactive images are skipped.
@@ -351,6 +355,10 @@ void lockstep_batch_run(nli_ctx *ctx, int n, const nli_process_params *params, c
                         const uint8_t *const *masks, const int32_t *widths, const int32_t *heights,
                         const int32_t *channels, float *const *outputs, nli_process_stats *stats, int32_t *status,
                         bool host_buffers);
+// batch.cu: a worker context of a batch (its own stream and workspace), and
+// the merge of its profile and counters into the parent
+nli_ctx *new_worker(int device);
+void merge_worker(nli_ctx *parent, nli_ctx *w);
 
 // Records of the checked build's bounds tests, one per translation unit
 // with instrumented kernels (0 elsewhere; read and cleared).

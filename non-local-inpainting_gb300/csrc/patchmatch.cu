@@ -138,6 +138,11 @@ struct PmArgs {
 	// lanes per candidate, candidates per warp step, window rows
 	int L, K, rows;
 	float lambda, lambda_d;
+	// patch-mean lower bound (null: off): the weighted patch means of the
+	// padded source and target, one float4 per (W + 1) x (H + 1) position,
+	// and the largest absolute pixel value of the images (as float bits)
+	const float4 *smom, *tmom;
+	const unsigned *vmax;
 };
 
 // Philox key of this PatchMatch call: the seed mixed with the call's index
@@ -194,14 +199,17 @@ __device__ __forceinline__ void load_weights(const DistArgs &a, float *s_w)
 // The warp's target window: rows x L pixels starting at the patch corner.
 // With up to 3 channels the unused fourth component carries the tap's
 // weight (0 outside the patch), so the distance reads one float4 per row.
-template <int C>
+template <int KIND, int C, int P>
 __device__ __forceinline__ void load_window(const PmArgs &p, const float *s_w, int x, int y, float4 *s_t)
 {
 	const int lane = threadIdx.x & 31;
-	const int px = p.rx + p.ex, py = p.ry + p.ey;
+	// compiled sizes for P x P patches (a division by a constant), else the call's
+	constexpr int LP = P ? P + (Kind<KIND>::grad ? 1 : 0) : 1;
+	const int L = P ? LP : p.L, rows = P ? LP : p.rows;
+	const int px = P ? P : p.rx + p.ex, py = P ? P : p.ry + p.ey;
 	const float4 *T = p.tgt + (size_t)(y - p.ry) * p.tWp + (x - p.rx);
-	for (int e = lane; e < p.rows * p.L; e += 32) {
-		const int r = e / p.L, c = e - r * p.L;
+	for (int e = lane; e < rows * L; e += 32) {
+		const int r = P ? e / LP : e / L, c = e - r * L;
 		float4 v = __ldg(T + (size_t)r * p.tWp + c);
 		if (C <= 3) v.w = (r < py && c < px) ? s_w[r * px + c] : 0.f;
 		s_t[e] = v;
@@ -340,6 +348,104 @@ __device__ __forceinline__ float combine(const Acc &A, const PmArgs &p)
 	float v = fmaf(p.lambda, A.n, (1.0f - p.lambda) * A.g);
 	if (KIND == NLI_DIST_L2_RGBD) v = fmaf(p.lambda_d, A.nd, fmaf(1.0f - p.lambda_d, A.gd, v));
 	return v;
+}
+
+// ------------------------------------------------ patch-mean lower bound
+// Jensen's inequality gives, for weights v_k >= 0 summing to V,
+//   sum_k v_k |d_k|^2 >= |sum_k v_k d_k|^2 / V,   sum_k v_k |d_k|_1 >= |sum_k v_k d_k|_1.
+// With the kernel's tap weights v_k = w_k / P (sum 1 / P) and d_k the colour
+// or gradient difference of tap k, sum_k w_k d_k is the difference of the
+// two patches' weighted means of the image or of its forward differences;
+// the mean of the differences is the difference of means one column (row)
+// apart.  So a candidate whose patch means differ enough from the target's
+// cannot beat the current match and is not evaluated.  Exactness: every
+// mean difference is shrunk by a slack (2e-4 of the largest pixel value)
+// that covers the float rounding of the means and of the kernel's per-tap
+// differences, and the bound must exceed the current distance by a 1e-4
+// relative margin that covers the rounding of the kernel's sums; the field
+// and distances are those of evaluating every candidate.
+__device__ __forceinline__ float shrink(float v, float slack) { return fmaxf(fabsf(v) - slack, 0.f); }
+
+// True when candidate (cx, cy) for target (x, y) provably cannot reach a
+// distance below bd.  The target's means are read here too (the same
+// address in every lane), so nothing stays live across the evaluations.
+template <int KIND, int C>
+__device__ __forceinline__ bool bound_rejects(const PmArgs &p, int x, int y, int cx, int cy, float bd)
+{
+	const float4 *M = p.smom + (size_t)cy * p.sWp + cx;
+	const float4 m0 = __ldg(M), mx = __ldg(M + 1), my = __ldg(M + p.sWp);
+	const float4 *T = p.tmom + (size_t)y * p.tWp + x;
+	const float4 t0 = __ldg(T), txx = __ldg(T + 1), tyy = __ldg(T + p.tWp);
+	const float slack = 2e-4f * __uint_as_float(__ldg(p.vmax));
+	const float mc[4] = {m0.x, m0.y, m0.z, m0.w}, tc[4] = {t0.x, t0.y, t0.z, t0.w};
+	const float sx[4] = {mx.x - m0.x, mx.y - m0.y, mx.z - m0.z, mx.w - m0.w};
+	const float sy[4] = {my.x - m0.x, my.y - m0.y, my.z - m0.z, my.w - m0.w};
+	const float tx[4] = {txx.x - t0.x, txx.y - t0.y, txx.z - t0.z, txx.w - t0.w};
+	const float ty[4] = {tyy.x - t0.x, tyy.y - t0.y, tyy.z - t0.z, tyy.w - t0.w};
+	float col = 0.f, grad = 0.f, dcol = 0.f, dgrad = 0.f;
+#pragma unroll
+	for (int c = 0; c < C; c++) {
+		const float dc = shrink(mc[c] - tc[c], slack);
+		const bool depth = KIND == NLI_DIST_L2_RGBD && c == 3;
+		if (KIND == NLI_DIST_L1_NORM) {
+			col += dc;
+			continue;
+		}
+		if (depth)
+			dcol = dc * dc;
+		else
+			col = fmaf(dc, dc, col);
+		if (Kind<KIND>::grad) {
+			const float gx = shrink(sx[c] - tx[c], slack), gy = shrink(sy[c] - ty[c], slack);
+			const float g = fmaf(gx, gx, gy * gy);
+			if (depth)
+				dgrad = g;
+			else
+				grad += g;
+		}
+	}
+	float lb = col;
+	if (Kind<KIND>::grad) lb = fmaf(p.lambda, col, (1.0f - p.lambda) * grad);
+	if (KIND == NLI_DIST_L2_RGBD) lb = fmaf(p.lambda_d, dcol, fmaf(1.0f - p.lambda_d, dgrad, lb));
+	const float P = (float)((p.rx + p.ex) * (p.ry + p.ey));
+	return lb * (1.0f - 1e-4f) >= bd * P;
+}
+
+// Weighted patch means of the padded image at every position of the
+// (W + 1) x (H + 1) grid (window clamped to the grid), and the largest
+// absolute pixel value (atomicMax on the float bits of non-negative values).
+__device__ __forceinline__ void moments_span(const DistArgs &a, const float4 *__restrict__ pad, int W, int H,
+                                             float4 *__restrict__ mom, unsigned *vmax, int first, int stride)
+{
+	const int Wp = W + 1, n = Wp * (H + 1);
+	float vm = 0.f;
+	for (int i = first; i < n; i += stride) {
+		const int y = i / Wp, x = i - y * Wp;
+		float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+		for (int dy = 0; dy < a.py; dy++) {
+			const int yy = min(max(y - a.ry + dy, 0), H);
+			for (int dx = 0; dx < a.px; dx++) {
+				const int xx = min(max(x - a.rx + dx, 0), W);
+				const float4 v = __ldg(pad + (size_t)yy * Wp + xx);
+				const float w = a.weights[dy * a.px + dx];
+				acc.x = fmaf(w, v.x, acc.x);
+				acc.y = fmaf(w, v.y, acc.y);
+				acc.z = fmaf(w, v.z, acc.z);
+				acc.w = fmaf(w, v.w, acc.w);
+			}
+		}
+		mom[i] = acc;
+		const float4 v = __ldg(pad + i);
+		vm = fmaxf(vm, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
+	}
+	for (int o = 16; o > 0; o >>= 1) vm = fmaxf(vm, __shfl_xor_sync(0xffffffffu, vm, o));
+	if ((threadIdx.x & 31) == 0 && vm > 0.f) atomicMax(vmax, __float_as_uint(vm));
+}
+
+__global__ void k_pm_moments(DistArgs a, const float4 *__restrict__ pad, int W, int H, float4 *__restrict__ mom,
+                             unsigned *vmax)
+{
+	moments_span(a, pad, W, H, mom, vmax, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 // Evaluates the n candidates held one per lane (packed x | y << 16, lane i
@@ -606,7 +712,7 @@ __device__ __forceinline__ void pm_init_point(const PmArgs &p, const PmSmem &m, 
 		if constexpr (V == kPmRegs)
 			load_window_regs<KIND, C, P>(p, m.w, x, y, tw);
 		else
-			load_window<C>(p, m.w, x, y, m.t);
+			load_window<KIND, C, P>(p, m.w, x, y, m.t);
 		eval_candidates<KIND, C, P, V>(p, m.w, m.t, n.x | (n.y << 16), 1, best, d, partial, &ts, tw);
 		evals++;
 		__syncwarp();
@@ -667,7 +773,8 @@ __device__ __forceinline__ void pm_sweep_point(const PmArgs &p, const PmSmem &m,
 		if constexpr (V == kPmRegs)
 			load_window_regs<KIND, C, P>(p, m.w, x, y, tw);
 		else
-			load_window<C>(p, m.w, x, y, m.t);
+			load_window<KIND, C, P>(p, m.w, x, y, m.t);
+		const bool bounded = p.smom != nullptr;
 		// propagation: lane 4s + k proposes the match of neighbour k
 		// (left, right, up, down) at distance 1 (s = 0) or at the jump
 		// distance (s = 1), shifted back by the neighbour's offset
@@ -681,7 +788,7 @@ __device__ __forceinline__ void pm_sweep_point(const PmArgs &p, const PmSmem &m,
 				const int2 q = nnf_in[ny * p.tW + nx];
 				if (q.x >= 0) {
 					const int cx = q.x + (x - nx), cy = q.y + (y - ny);
-					valid = src_ok(p, cx, cy);
+					valid = src_ok(p, cx, cy) && !(bounded && bound_rejects<KIND, C>(p, x, y, cx, cy, bd));
 					packed = cx | (cy << 16);
 				}
 			}
@@ -706,7 +813,7 @@ __device__ __forceinline__ void pm_sweep_point(const PmArgs &p, const PmSmem &m,
 				const int rx = x_min + rng.below(x_max - x_min);
 				const int ry = y_min + rng.below(y_max - y_min);
 				if (src_ok(p, rx, ry)) {
-					valid = true;
+					valid = !(bounded && bound_rejects<KIND, C>(p, x, y, rx, ry, bd));
 					packed = rx | (ry << 16);
 					max_shot = max(max_shot, t);
 					break;
@@ -1011,14 +1118,26 @@ __device__ __forceinline__ void pm_batch_count(unsigned long long *image, unsign
 	evals = partial = 0;
 }
 
-// The padded float4 pixels of every active image (k_pad4 per image).
+// The padded float4 pixels of every active image (k_pad4 per image); the
+// largest-value word of its patch means is cleared.
 __global__ void k_pad4_batch(const __grid_constant__ PmBatchArgs B, int C)
 {
 	const int t = blockIdx.y;
 	const PmBatchTask &T = B.t[t];
 	if (!batch_on(B.active, T.flag)) return;
+	if (T.p.vmax && blockIdx.x == 0 && threadIdx.x == 0) *const_cast<unsigned *>(T.p.vmax) = 0u;
 	pad4_span(T.img, T.p.sW, T.p.sH, C, const_cast<float4 *>(T.p.src), blockIdx.x * blockDim.x + threadIdx.x,
 	          gridDim.x * blockDim.x);
+}
+
+// The patch means of every active image (k_pm_moments per image).
+__global__ void k_pm_moments_batch(DistArgs a, const __grid_constant__ PmBatchArgs B)
+{
+	const int t = blockIdx.y;
+	const PmBatchTask &T = B.t[t];
+	if (!batch_on(B.active, T.flag) || !T.p.smom) return;
+	moments_span(a, T.p.src, T.p.sW, T.p.sH, const_cast<float4 *>(T.p.smom), const_cast<unsigned *>(T.p.vmax),
+	             blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
 }
 
 // k_fill_nnf per active image: the result field to "none", and the image's
@@ -1185,6 +1304,8 @@ void patchmatch_batch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli
 		p.lambda_d = a.lambda_d;
 		p.seed = it.seed;
 		p.calls = it.calls;
+		p.smom = p.tmom = it.mom;
+		p.vmax = it.mom ? it.vmax : nullptr;
 		T.flag = it.flag;
 		T.counter = it.counter;
 		T.img = it.img;
@@ -1203,6 +1324,11 @@ void patchmatch_batch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli
 	NLI_CHECK_LAUNCH();
 	k_fill_nnf_batch<<<dim3((unsigned)std::min((maxpix + per - 1) / per, 1024), (unsigned)n), per, 0, s>>>(B);
 	NLI_CHECK_LAUNCH();
+	if (B.t[0].p.smom) {
+		k_pm_moments_batch<<<dim3((unsigned)std::min((maxpad + per - 1) / per, 1024), (unsigned)n), per, 0, s>>>(a,
+		                                                                                                       B);
+		NLI_CHECK_LAUNCH();
+	}
 	if (maxnt == 0) return;
 	unsigned long long *counter = ctx->buf<unsigned long long>("pm.counter", 2);
 	const int taps = a.px * a.py;
@@ -1261,6 +1387,27 @@ void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patch
 		launch_pad4(s, tgt, tW, tH, C, t4);
 	}
 
+	// patch means for the lower bound (NLI_TUNE_PM_BOUND)
+	float4 *smom = nullptr, *tmom = nullptr;
+	unsigned *vmax = nullptr;
+	if (ctx->tune_pm_bound) {
+		DistArgs da;
+		fill_dist_args(da, dp, C);
+		vmax = ctx->buf<unsigned>("pm.vmax", 1);
+		NLI_CUDA(cudaMemsetAsync(vmax, 0, sizeof(unsigned), s));
+		smom = ctx->buf<float4>("pm.smom", (size_t)(sW + 1) * (sH + 1));
+		const int ns = (sW + 1) * (sH + 1);
+		k_pm_moments<<<(ns + 255) / 256, 256, 0, s>>>(da, s4, sW, sH, smom, vmax);
+		NLI_CHECK_LAUNCH();
+		tmom = smom;
+		if (t4 != s4) {
+			tmom = ctx->buf<float4>("pm.tmom", (size_t)(tW + 1) * (tH + 1));
+			const int nt4 = (tW + 1) * (tH + 1);
+			k_pm_moments<<<(nt4 + 255) / 256, 256, 0, s>>>(da, t4, tW, tH, tmom, vmax);
+			NLI_CHECK_LAUNCH();
+		}
+	}
+
 	if (!tlist) {
 		int32_t *l = ctx->buf<int32_t>("pm.tlist", nT);
 		n_target = compact_mask(ctx, tmask, tW, tH, l, "pm");
@@ -1310,6 +1457,9 @@ void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patch
 		p.lambda_d = a.lambda_d;
 		p.seed = ctx->seed;
 		p.calls = &ctx->status->pm_calls;  // advanced by k_fill_nnf above
+		p.smom = smom;
+		p.tmom = tmom;
+		p.vmax = vmax;
 		if (energy) NLI_CUDA(cudaMemsetAsync(counter, 0, 2 * sizeof(unsigned long long), s));
 		PmMetrics mt;
 		const int iters = std::max(pm.iterations, 0);

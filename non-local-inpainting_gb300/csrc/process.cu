@@ -4,8 +4,11 @@
 // iteration limit (inpaint_internal, :349-417), with propagate_weights
 // (:492-557) between scales.  Host code only sequences kernels and reads one
 // scalar per iteration for the stopping test.
+#include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <mutex>
+#include <thread>
 
 #include "nli_device.cuh"
 
@@ -173,6 +176,10 @@ struct Driver {
 		NLI_CUDA(cudaStreamSynchronize(ctx->stream));
 		L.source_empty = *(int *)ctx->host_pinned != 0;
 		L.prepared = true;
+		if (stats && l < NLI_MAX_SCALES) {
+			stats->targets[l] = L.nt;
+			stats->holes[l] = L.nh;
+		}
 	}
 
 	void pm(const float *img, const uint8_t *src, const Level &L, const int32_t *init, int32_t *out)
@@ -451,6 +458,7 @@ struct Driver {
 		ctx->candidates = cand0 + (int64_t)hc[0];
 		ctx->candidates_partial += (int64_t)hc[1];
 		if (stats) {
+			stats->candidates_partial = (int64_t)hc[1];
 			stats->patchmatch_calls = pm_calls;
 			stats->update_calls = upd_calls;
 			stats->cg_iterations = ctx->cg_iterations - cg0;
@@ -592,8 +600,9 @@ struct LkImage {
 	std::vector<LkLevel> lv;
 	float *orig = nullptr, *up = nullptr;
 	int32_t *A = nullptr, *B = nullptr, *nnf_l = nullptr, *scaled = nullptr, *nnf_y = nullptr;
-	float4 *pad = nullptr;
+	float4 *pad = nullptr, *mom = nullptr;
 	float *dist_x = nullptr, *dist_y = nullptr;
+	unsigned *vmax = nullptr;
 	int64_t pm_calls = 0, upd_calls = 0, graph_iters = 0;
 	bool ok() const { return status == NLI_OK; }
 };
@@ -676,8 +685,10 @@ class Lockstep {
 			m.scaled = a.take<int32_t>(2 * n0);
 			m.nnf_y = a.take<int32_t>(2 * n0);
 			m.pad = a.take<float4>((size_t)(m.W + 1) * (m.H + 1));
+			m.mom = a.take<float4>((size_t)(m.W + 1) * (m.H + 1));
 			m.dist_x = a.take<float>(n0);
 			m.dist_y = a.take<float>(n0);
+			m.vmax = a.take<unsigned>(1);
 			if (pass == 0) arena_size[g] = a.off + 256;
 		}
 	}
@@ -726,6 +737,10 @@ class Lockstep {
 			NLI_CUDA(cudaMemcpyAsync(ctx->host_pinned, empty, sizeof(int), cudaMemcpyDeviceToHost, s));
 			NLI_CUDA(cudaStreamSynchronize(s));
 			L.source_empty = *(int *)ctx->host_pinned != 0;
+			if (m.stats && l < NLI_MAX_SCALES) {
+				m.stats->targets[l] = L.nt;
+				m.stats->holes[l] = L.nh;
+			}
 		}
 	}
 
@@ -753,6 +768,8 @@ class Lockstep {
 		it.calls = &dev->calls[g];
 		it.counter = dev->cand[g];
 		it.flag = g;
+		it.mom = ctx->tune_pm_bound ? m.mom : nullptr;
+		it.vmax = m.vmax;
 		if (count) m.pm_calls++;
 		return it;
 	}
@@ -1095,6 +1112,7 @@ class Lockstep {
 					m.stats->update_calls = m.upd_calls;
 					m.stats->graph_iterations = m.graph_iters;
 					m.stats->candidates = (int64_t)h->cand[g][0];
+					m.stats->candidates_partial = (int64_t)h->cand[g][1];
 				}
 			}
 		} catch (...) {
@@ -1119,6 +1137,67 @@ static bool same_group(const nli_process_params &a, int Ca, const nli_process_pa
 	       a.update.sigma == b.update.sigma;
 }
 
+// Pixels over an image's whole pyramid: the load estimate by which a
+// group's images are dealt into concurrent sub-groups.
+static double pyramid_pixels(const nli_process_params &p, int W, int H)
+{
+	double total = 0.0;
+	for (int i = 0; i < std::max(1, std::min(p.scales, NLI_MAX_SCALES)); i++) {
+		total += (double)W * H;
+		if (!(p.subsampling_rate > 0.f && p.subsampling_rate < 1.f)) break;
+		W = sample_size_host(W, p.subsampling_rate);
+		H = sample_size_host(H, p.subsampling_rate);
+	}
+	return total;
+}
+
+// Runs one lockstep group -- images `grp`, all of channel count C -- on
+// context `c` (the caller's or a worker), writing each image's status.
+static void lockstep_group_run(nli_ctx *c, const std::vector<int> &grp, int C, uint64_t seed,
+                               const nli_process_params *params, const float *const *images,
+                               const uint8_t *const *masks, const int32_t *widths, const int32_t *heights,
+                               float *const *outputs, nli_process_stats *stats, bool host_buffers,
+                               std::vector<int> &rcs, std::vector<std::string> &errors)
+{
+	cudaStream_t s = c->stream;
+	Lockstep L(c, C);
+	L.im.resize(grp.size());
+	for (size_t g = 0; g < grp.size(); g++) {
+		const int i = grp[g];
+		LkImage &m = L.im[g];
+		m.idx = i;
+		m.p = &params[i];
+		m.W = widths[i];
+		m.H = heights[i];
+		m.stats = stats ? stats + i : nullptr;
+		m.seed = batch_seed(seed, i);
+		if (host_buffers) {
+			const size_t np = (size_t)m.W * m.H;
+			float *d_img = c->buf<float>("lk." + std::to_string(g) + ".in", np * C);
+			uint8_t *d_mask = c->buf<uint8_t>("lk." + std::to_string(g) + ".inmask", np);
+			m.out = c->buf<float>("lk." + std::to_string(g) + ".out", np * C);
+			NLI_CUDA(cudaMemcpyAsync(d_img, images[i], np * C * sizeof(float), cudaMemcpyHostToDevice, s));
+			NLI_CUDA(cudaMemcpyAsync(d_mask, masks[i], np, cudaMemcpyHostToDevice, s));
+			m.in = d_img;
+			m.in_mask = d_mask;
+		} else {
+			m.in = images[i];
+			m.in_mask = masks[i];
+			m.out = outputs[i];
+		}
+	}
+	L.run();
+	for (size_t g = 0; g < grp.size(); g++) {
+		const LkImage &m = L.im[g];
+		rcs[m.idx] = m.status;
+		errors[m.idx] = m.error;
+		if (host_buffers && m.ok())
+			NLI_CUDA(cudaMemcpyAsync(outputs[m.idx], m.out, (size_t)m.W * m.H * C * sizeof(float),
+			                         cudaMemcpyDeviceToHost, s));
+	}
+	if (host_buffers) NLI_CUDA(cudaStreamSynchronize(s));
+}
+
 void lockstep_batch_run(nli_ctx *ctx, int n, const nli_process_params *params, const float *const *images,
                         const uint8_t *const *masks, const int32_t *widths, const int32_t *heights,
                         const int32_t *channels, float *const *outputs, nli_process_stats *stats, int32_t *status,
@@ -1128,7 +1207,6 @@ void lockstep_batch_run(nli_ctx *ctx, int n, const nli_process_params *params, c
 	std::vector<std::string> errors(n);
 	std::vector<int> rcs(n, NLI_OK);
 	std::vector<bool> placed(n, false);
-	cudaStream_t s = ctx->stream;
 	for (int i = 0; i < n; i++) {
 		if (!images[i] || !masks[i] || !outputs[i]) {
 			rcs[i] = NLI_E_INVALID;
@@ -1154,42 +1232,72 @@ void lockstep_batch_run(nli_ctx *ctx, int n, const nli_process_params *params, c
 				placed[i] = true;
 			}
 		const int C = channels[first];
-		Lockstep L(ctx, C);
-		L.im.resize(grp.size());
-		for (size_t g = 0; g < grp.size(); g++) {
-			const int i = grp[g];
-			LkImage &m = L.im[g];
-			m.idx = i;
-			m.p = &params[i];
-			m.W = widths[i];
-			m.H = heights[i];
-			m.stats = stats ? stats + i : nullptr;
-			m.seed = batch_seed(ctx->seed, i);
-			if (host_buffers) {
-				const size_t np = (size_t)m.W * m.H;
-				float *d_img = ctx->buf<float>("lk." + std::to_string(g) + ".in", np * C);
-				uint8_t *d_mask = ctx->buf<uint8_t>("lk." + std::to_string(g) + ".inmask", np);
-				m.out = ctx->buf<float>("lk." + std::to_string(g) + ".out", np * C);
-				NLI_CUDA(cudaMemcpyAsync(d_img, images[i], np * C * sizeof(float), cudaMemcpyHostToDevice, s));
-				NLI_CUDA(cudaMemcpyAsync(d_mask, masks[i], np, cudaMemcpyHostToDevice, s));
-				m.in = d_img;
-				m.in_mask = d_mask;
-			} else {
-				m.in = images[i];
-				m.in_mask = masks[i];
-				m.out = outputs[i];
+		const int k = std::max(1, std::min(ctx->tune_batch_groups, (int)grp.size()));
+		if (k == 1) {
+			lockstep_group_run(ctx, grp, C, ctx->seed, params, images, masks, widths, heights, outputs, stats,
+			                   host_buffers, rcs, errors);
+			continue;
+		}
+		// deal the images, largest pyramid first, each to the least-loaded
+		// sub-group; every sub-group runs on a worker context of its own
+		std::vector<int> order = grp;
+		std::vector<double> load(n, 0.0);
+		for (int i : grp) load[i] = pyramid_pixels(params[i], widths[i], heights[i]);
+		std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return load[a] > load[b]; });
+		std::vector<std::vector<int>> sub(k);
+		std::vector<double> sum(k, 0.0);
+		for (int i : order) {
+			const int t = (int)(std::min_element(sum.begin(), sum.end()) - sum.begin());
+			sub[t].push_back(i);
+			sum[t] += load[i];
+		}
+		for (auto &v : sub) std::sort(v.begin(), v.end());
+		while ((int)ctx->workers.size() < k) ctx->workers.push_back(new_worker(ctx->device));
+		// device inputs may come from work queued on the caller's stream
+		cudaEvent_t ready = nullptr;
+		NLI_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+		NLI_CUDA(cudaEventRecord(ready, ctx->stream));
+		std::mutex fatal_lock;
+		bool fatal = false;
+		Error fatal_error{NLI_OK, ""};
+		auto work = [&](int t) {
+			nli_ctx *w = ctx->workers[t];
+			try {
+				NLI_CUDA(cudaSetDevice(w->device));
+				w->profiling = ctx->profiling;
+				w->tune_cg_cluster_cap = ctx->tune_cg_cluster_cap;
+				w->tune_cg_unknowns_per_cta = ctx->tune_cg_unknowns_per_cta;
+				w->tune_pm_variant = ctx->tune_pm_variant;
+				w->tune_cg_precond = ctx->tune_cg_precond;
+				w->tune_graph_loop = ctx->tune_graph_loop;
+				w->tune_cg_single_max = ctx->tune_cg_single_max;
+				w->tune_pm_bound = ctx->tune_pm_bound;
+				NLI_CUDA(cudaStreamWaitEvent(w->stream, ready, 0));
+				lockstep_group_run(w, sub[t], C, ctx->seed, params, images, masks, widths, heights, outputs,
+				                   stats, host_buffers, rcs, errors);
+			} catch (const Error &e) {
+				std::lock_guard<std::mutex> g(fatal_lock);
+				if (!fatal) fatal_error = e;
+				fatal = true;
+			} catch (const std::bad_alloc &) {
+				std::lock_guard<std::mutex> g(fatal_lock);
+				if (!fatal) fatal_error = Error{NLI_E_NOMEM, "host allocation failed"};
+				fatal = true;
 			}
+		};
+		std::vector<std::thread> threads;
+		for (int t = 1; t < k; t++) threads.emplace_back(work, t);
+		work(0);
+		for (auto &th : threads) th.join();
+		// the caller's stream continues after every sub-group's work
+		for (int t = 0; t < k; t++) {
+			nli_ctx *w = ctx->workers[t];
+			NLI_CUDA(cudaEventRecord(ready, w->stream));
+			NLI_CUDA(cudaStreamWaitEvent(ctx->stream, ready, 0));
+			merge_worker(ctx, w);
 		}
-		L.run();
-		for (size_t g = 0; g < grp.size(); g++) {
-			const LkImage &m = L.im[g];
-			rcs[m.idx] = m.status;
-			errors[m.idx] = m.error;
-			if (host_buffers && m.ok())
-				NLI_CUDA(cudaMemcpyAsync(outputs[m.idx], m.out, (size_t)m.W * m.H * C * sizeof(float),
-				                         cudaMemcpyDeviceToHost, s));
-		}
-		if (host_buffers) NLI_CUDA(cudaStreamSynchronize(s));
+		NLI_CUDA(cudaEventDestroy(ready));
+		if (fatal) throw fatal_error;
 	}
 	if (status)
 		for (int i = 0; i < n; i++) status[i] = rcs[i];

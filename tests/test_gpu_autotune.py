@@ -1,5 +1,6 @@
-"""The autotuner's CG launch shapes: every candidate gives the same update
-up to the rounding of the CG sums, and the chosen shape is applied."""
+"""The autotuner: every CG launch shape gives the same update up to the
+rounding of the CG sums, the PatchMatch variants and bound and the batch
+forms give identical results, and each tuner applies its choice."""
 import numpy as np
 import pytest
 
@@ -63,3 +64,37 @@ def test_cache_file_round_trip(gpu_ctx, tmp_path):
         assert autotune.load(gpu_ctx, path, "missing") is None
     finally:
         autotune.apply(gpu_ctx, cg=(16, 1024), batch_width=8, pm_variant=0)
+
+
+def test_tune_cg_single_and_pm_bound(gpu_ctx):
+    from nli_gb300 import autotune
+    cases = [autotune.poisson_case(gpu_ctx, size=s, seed=1) for s in (48, 96)]
+    res = autotune.tune_cg_single(gpu_ctx, cases, limits=(0, 1024, 4096), repeats=1)
+    assert sorted(res["ms"]) == [0, 1024, 4096]
+    assert gpu_ctx.get_tuning(gpu_ctx.TUNE_CG_SINGLE_MAX) == res["best"]
+    case = autotune.patchmatch_case(gpu_ctx, size=160, seed=2)
+    res = autotune.tune_pm_bound(gpu_ctx, case, repeats=1)
+    assert sorted(res["ms"]) == [0, 1]
+    assert gpu_ctx.get_tuning(gpu_ctx.TUNE_PM_BOUND) == res["best"]
+    autotune.apply(gpu_ctx, cg_single=1024, pm_bound=1)
+
+
+def test_tune_batch_mode_and_groups(gpu_ctx):
+    import torch
+    from nli_gb300 import autotune
+    from nli_gb300 import workloads as wl
+    rng = np.random.default_rng(4)
+    items, params = [], []
+    for i in range(6):
+        w, h = int(rng.integers(48, 96)), int(rng.integers(48, 96))
+        img, _ = wl.voronoi_texture(w, h, 8, rng)
+        mask = wl.ellipse_mask(w, h, 2, 0.1, rng)
+        items.append((torch.from_numpy(img).cuda(), torch.from_numpy(mask).cuda()))
+        params.append(wl.params("nlmeans" if i % 2 else "nlpoisson", scales=2, coarse=0.5, iters=4, cg_tol=1e-4))
+    try:
+        res = autotune.tune_batch_mode(gpu_ctx, items, params)
+        assert sorted(res["ms"]) == [0, 1] and gpu_ctx.get_tuning(gpu_ctx.TUNE_BATCH_MODE) == res["best"]
+        res = autotune.tune_batch_groups(gpu_ctx, items, params, groups=(1, 3))
+        assert sorted(res["ms"]) == [1, 3] and gpu_ctx.get_tuning(gpu_ctx.TUNE_BATCH_GROUPS) == res["best"]
+    finally:
+        autotune.apply(gpu_ctx, batch_mode=1, batch_groups=2)

@@ -5,11 +5,15 @@ output for the same inputs: three input seeds per configuration
 with srand(101) by tests/golden/make_golden.py --full --seeds).
 
 The GPU PatchMatch draws different random numbers and sweeps in parallel,
-so the inpainting reaches a different (similar) solution.  The contract is
-the metric's: the hole-region PSNR of the GPU output against the ground
-truth (the synthetic image before masking) may not fall more than 0.1 dB
-below the reference's, as the mean over the seeds, per channel group.  The
-per-seed figures are printed."""
+so the inpainting reaches a different (similar) solution; like the
+reference's own runs with different seeds, runs with different PatchMatch
+seeds differ in hole PSNR by a few tenths of a dB.  The contract is the
+metric's: the hole-region PSNR of the GPU output against the ground truth
+(the synthetic image before masking) may not fall more than 0.1 dB below
+the reference's.  It is tested on means: per input seed, the mean over
+eight GPU PatchMatch seeds (the reference has one run per input); then the
+mean over the three input seeds of (reference - GPU), per channel group.
+The per-run figures are printed."""
 import json
 import os
 
@@ -21,7 +25,8 @@ from conftest import GOLDEN
 pytestmark = pytest.mark.gpu
 
 SEEDS = (0, 1, 2)
-MAX_GAP_DB = 0.1  # reference PSNR minus ours, mean over the seeds
+PM_SEEDS = tuple(range(101, 109))  # GPU PatchMatch seeds per input
+MAX_GAP_DB = 0.1  # reference PSNR minus ours, mean over the input seeds
 
 
 def psnr(a, b, peak):
@@ -37,22 +42,24 @@ def run_seed(gpu_ctx, name, seed):
     from nli_gb300 import workloads as wl
     g = np.load(reference_path(name, seed))
     img, mask, p = getattr(wl, name)(seed=seed)
-    gpu_ctx.set_seed(101)
-    out, st = gpu_ctx.process(img, mask, p)
     hole = mask > 0
-    assert np.isfinite(out).all()
-    assert np.array_equal(out[~hole], img[~hole])
     ref_hole = g["hole"]
-    rows = []
     # colour channels on a 0-255 peak; the depth channel of configuration 3
     # (metres) on its own range
     chans = [(slice(0, 3), 255.0)]
     if img.shape[2] == 4:
         chans.append((slice(3, 4), float(img[..., 3].max() - img[..., 3].min())))
-    for sl, peak in chans:
-        o, r, t = out[hole][:, sl], ref_hole[:, sl], img[hole][:, sl]
-        rows.append({"seed": seed, "channels": "%d:%d" % (sl.start, sl.stop), "psnr_gpu_vs_ref": psnr(o, r, peak),
-                     "psnr_gpu_vs_truth": psnr(o, t, peak), "psnr_ref_vs_truth": psnr(r, t, peak)})
+    rows = []
+    for pm_seed in PM_SEEDS:
+        gpu_ctx.set_seed(pm_seed)
+        out, st = gpu_ctx.process(img, mask, p)
+        assert np.isfinite(out).all()
+        assert np.array_equal(out[~hole], img[~hole])
+        for sl, peak in chans:
+            o, r, t = out[hole][:, sl], ref_hole[:, sl], img[hole][:, sl]
+            rows.append({"seed": seed, "pm_seed": pm_seed, "channels": "%d:%d" % (sl.start, sl.stop),
+                         "psnr_gpu_vs_ref": psnr(o, r, peak), "psnr_gpu_vs_truth": psnr(o, t, peak),
+                         "psnr_ref_vs_truth": psnr(r, t, peak)})
     return rows, st
 
 
@@ -65,11 +72,16 @@ def test_full_size_vs_reference(gpu_ctx, name):
     groups = sorted({r["channels"] for r in rows})
     summary = []
     for ch in groups:
-        sel = [r for r in rows if r["channels"] == ch]
-        gpu = float(np.mean([r["psnr_gpu_vs_truth"] for r in sel]))
-        ref = float(np.mean([r["psnr_ref_vs_truth"] for r in sel]))
-        summary.append({"channels": ch, "mean_psnr_gpu_vs_truth": gpu, "mean_psnr_ref_vs_truth": ref,
-                        "mean_gap_db": ref - gpu})
+        per_input = []
+        for seed in SEEDS:
+            sel = [r for r in rows if r["channels"] == ch and r["seed"] == seed]
+            per_input.append((float(np.mean([r["psnr_gpu_vs_truth"] for r in sel])), sel[0]["psnr_ref_vs_truth"],
+                              float(np.std([r["psnr_gpu_vs_truth"] for r in sel]))))
+        gpu = float(np.mean([a for a, _, _ in per_input]))
+        ref = float(np.mean([b for _, b, _ in per_input]))
+        summary.append({"channels": ch, "per_input": [{"seed": s, "gpu_mean": a, "gpu_std": c, "reference": b}
+                                                      for s, (a, b, c) in zip(SEEDS, per_input)],
+                        "mean_psnr_gpu_vs_truth": gpu, "mean_psnr_ref_vs_truth": ref, "mean_gap_db": ref - gpu})
     print(json.dumps({"workload": name, "seeds": list(SEEDS), "rows": rows, "summary": summary}))
     for r in rows:
         # a sanity bound per seed: the two outputs are the same kind of fill

@@ -1,6 +1,7 @@
 """Lockstep batches (NLI_TUNE_BATCH_MODE 1, the default): the images of a
 batch walk their pyramids together, one launch per kernel per pyramid rank
-covering every image, each rank's iteration loop one CUDA graph.  Every
+covering every image, each rank's iteration loop one CUDA graph, and the
+sub-groups of a group running concurrently on worker contexts.  Every
 image must equal its plain nli_process run with the per-image seed bit for
 bit -- output and statistics -- whatever the mix of sizes, methods, channel
 counts and parameters (images that cannot share launches form separate
@@ -11,7 +12,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 STAT_KEYS = ("scales", "width", "height", "iterations", "last_difference", "patchmatch_calls", "update_calls",
-             "cg_iterations", "candidates")
+             "cg_iterations", "candidates", "candidates_partial", "targets", "holes")
 
 
 def mixed_batch(seed=21, count=8):
@@ -170,3 +171,24 @@ def test_single_cta_cg_threshold(gpu_ctx, single_max):
         gpu_ctx.set_tuning(gpu_ctx.TUNE_CG_SINGLE_MAX, 1024)
     for i in range(len(items)):
         assert np.array_equal(got[i], want[i]), i
+
+
+@pytest.mark.parametrize("groups", [1, 3, 16])
+def test_lockstep_concurrent_groups(gpu_ctx, groups):
+    """Sub-groups of one launch-sharing group run concurrently on worker
+    contexts (NLI_TUNE_BATCH_GROUPS); every image still equals its plain
+    run, with host and with device buffers, and the per-image statistics
+    and the context's counters are those of the plain runs."""
+    items, params = mixed_batch(seed=27, count=8)
+    want, wst = plain(gpu_ctx, items, params, 61)
+    gpu_ctx.set_tuning(gpu_ctx.TUNE_BATCH_GROUPS, groups)
+    try:
+        got, gst = lockstep(gpu_ctx, items, params, 61)
+        gpu_ctx.set_seed(61)
+        dev, _ = gpu_ctx.process_batch_device(items, params)
+    finally:
+        gpu_ctx.set_tuning(gpu_ctx.TUNE_BATCH_GROUPS, 2)
+    for i in range(len(items)):
+        assert np.array_equal(got[i], want[i]), i
+        assert np.array_equal(dev[i].cpu().numpy(), want[i]), i
+        same_stats(gst[i], wst[i])

@@ -163,3 +163,147 @@ def poisson(u, lam, sigma, nnf, dom, ext, conf, px=9, py=9, lam_channels=None, s
             delta = torch.from_numpy(spl.spsolve(A.tocsc(), b.detach().numpy()))
         out[ys, xs, c] = o[ys, xs] + delta
     return out
+
+
+# --------------------------------------------------------------- fast path
+# The same FP64 expressions, vectorised for full-size finite differences
+# (no autograd): the gather structure of a case -- which centre and which
+# source pixel every (pixel, tap) pair reads -- is built once, and each
+# evaluation is a few weighted bincounts and one sparse factorisation.
+class Plan:
+    """Gather structure of one (nnf, dom, ext, conf) case."""
+
+    def __init__(self, nnf, dom, ext, conf, px=9, py=9):
+        H, W = dom.shape
+        self.H, self.W, self.px, self.py = H, W, px, py
+        hx, hy = px // 2, py // 2
+        self.dom = np.asarray(dom, bool)
+        conf = np.ones((H, W)) if conf is None else np.asarray(conf, np.float64)
+        ys, xs = np.nonzero(self.dom)
+        self.ys, self.xs = ys, xs
+        nh = len(ys)
+        self.index = -np.ones((H, W), np.int64)
+        self.index[ys, xs] = np.arange(nh)
+        # NL-means: per hole pixel, the window pixels (ii, jj) with a match
+        mi, mk, msrc, ms = [], [], [], []
+        xa, ya = np.maximum(xs - hx, 0), np.maximum(ys - hy, 0)
+        xb, yb = np.minimum(xs + hx, W - 1), np.minimum(ys + hy, H - 1)
+        for dy in range(-hy, hy + 1):
+            for dx in range(-hx, hx + 1):
+                ii, jj = xs + dx, ys + dy
+                inside = (ii >= xa) & (ii <= xb) & (jj >= ya) & (jj <= yb)
+                iic, jjc = np.clip(ii, 0, W - 1), np.clip(jj, 0, H - 1)
+                q = nnf[jjc, iic]
+                qx, qy = q[:, 0] + xs - iic, q[:, 1] + ys - jjc
+                ok = inside & (q[:, 0] != -1) & (qx >= 0) & (qy >= 0) & (qx < W) & (qy < H)
+                k = (jjc - ya) * px + (iic - xa)
+                cf = np.where(self.dom[jjc, iic], conf[jjc, iic], 1.0)
+                mi.append(np.nonzero(ok)[0])
+                mk.append(k[ok])
+                msrc.append(qy[ok] * W + qx[ok])
+                ms.append(cf[ok])
+        self.m_i = np.concatenate(mi)
+        self.m_k = np.concatenate(mk)
+        self.m_src = np.concatenate(msrc)
+        self.m_conf = np.concatenate(ms)
+        # NL-Poisson: per pixel q (every pixel), the taps with a valid centre
+        qy_, qx_ = np.mgrid[0:H, 0:W]
+        pi, pk, psrc, pc = [], [], [], []
+        ext = np.asarray(ext) != 0
+        for dy in range(-hy, hy + 1):
+            for dx in range(-hx, hx + 1):
+                cx, cy = qx_ - dx, qy_ - dy
+                ok = (cx >= 0) & (cy >= 0) & (cx < W) & (cy < H)
+                cxc, cyc = np.clip(cx, 0, W - 1), np.clip(cy, 0, H - 1)
+                ok &= ext[cyc, cxc]
+                nb = nnf[cyc, cxc]
+                nx, ny = nb[..., 0] + dx, nb[..., 1] + dy
+                ok &= (nx >= 0) & (ny >= 0) & (nx < W) & (ny < H)
+                sel = np.nonzero(ok.reshape(-1))[0]
+                pi.append(sel)
+                pk.append(np.full(len(sel), (dy + hy) * px + (dx + hx), np.int64))
+                psrc.append((ny * W + nx).reshape(-1)[sel])
+                pc.append(conf[cyc, cxc].reshape(-1)[sel])
+        self.p_i = np.concatenate(pi)
+        self.p_k = np.concatenate(pk)
+        self.p_src = np.concatenate(psrc)
+        self.p_conf = np.concatenate(pc)
+
+    def weights(self, sigma):
+        return patch_weights(float(sigma), self.px, self.py).numpy()
+
+
+def means_fast(u, sigma, plan):
+    """NL-means of `means` on the plan's case; u: (H, W, C) float64 array."""
+    H, W, C = u.shape
+    g = plan.weights(sigma)
+    w = g[plan.m_k] * plan.m_conf
+    nh = len(plan.ys)
+    den = np.bincount(plan.m_i, weights=w, minlength=nh)
+    flat = u.reshape(-1, C)
+    out = u.copy()
+    has = den > 0
+    for c in range(C):
+        num = np.bincount(plan.m_i, weights=w * flat[plan.m_src, c], minlength=nh)
+        vals = out[plan.ys, plan.xs, c]
+        vals[has] = num[has] / den[has]
+        out[plan.ys, plan.xs, c] = vals
+    return out
+
+
+def poisson_fast(u, lam, sigma, plan, lam_channels=None):
+    """NL-Poisson / NL-depth of `poisson` on the plan's case (direct sparse
+    solve, one factorisation per distinct lambda)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+    H, W, C = u.shape
+    n = H * W
+    g = plan.weights(sigma)
+    w = g[plan.p_k] * plan.p_conf
+    flat = u.reshape(-1, C)
+    gx = np.zeros_like(u)
+    gy = np.zeros_like(u)
+    gx[:, :-1] = u[:, 1:] - u[:, :-1]
+    gy[:-1, :] = u[1:, :] - u[:-1, :]
+    gxf, gyf = gx.reshape(-1, C), gy.reshape(-1, C)
+    S = np.bincount(plan.p_i, weights=w, minlength=n).reshape(H, W)
+    ys, xs = plan.ys, plan.xs
+    nh = len(ys)
+    Sk = S[ys, xs]
+    links = []
+    for (ddx, ddy, kind) in ((0, -1, "up"), (-1, 0, "left"), (0, 1, "down"), (1, 0, "right")):
+        nx, ny = xs + ddx, ys + ddy
+        inside = (nx >= 0) & (ny >= 0) & (nx < W) & (ny < H)
+        if kind == "up":
+            s = np.where(inside, S[np.maximum(ny, 0), xs], 0.0)
+        elif kind == "left":
+            s = np.where(inside, S[ys, np.maximum(nx, 0)], 0.0)
+        else:
+            s = np.where(inside, Sk, 0.0)
+        nxc, nyc = np.clip(nx, 0, W - 1), np.clip(ny, 0, H - 1)
+        links.append((s, nxc, nyc, np.where(inside, plan.index[nyc, nxc], -1)))
+    out = u.copy()
+    factors = {}
+    for c in range(C):
+        lc = float(lam if lam_channels is None else lam_channels[c])
+        oml = 1.0 - lc
+        U = np.bincount(plan.p_i, weights=w * flat[plan.p_src, c], minlength=n).reshape(H, W)
+        GX = np.bincount(plan.p_i, weights=w * gxf[plan.p_src, c], minlength=n).reshape(H, W)
+        GY = np.bincount(plan.p_i, weights=w * gyf[plan.p_src, c], minlength=n).reshape(H, W)
+        o = u[..., c]
+        D = np.where(xs != W - 1, GX[ys, xs], 0.0) - np.where(xs != 0, GX[ys, np.maximum(xs - 1, 0)], 0.0)
+        D += np.where(ys != H - 1, GY[ys, xs], 0.0) - np.where(ys != 0, GY[np.maximum(ys - 1, 0), xs], 0.0)
+        b = lc * U[ys, xs] - oml * D - lc * Sk * o[ys, xs]
+        for s, nxc, nyc, _ in links:
+            b = b + oml * s * (o[nyc, nxc] - o[ys, xs])
+        if lc not in factors:
+            rows, cols, vals = [np.arange(nh)], [np.arange(nh)], [lc * Sk + oml * sum(l[0] for l in links)]
+            for s, _, _, nbk in links:
+                m = nbk >= 0
+                rows.append(np.nonzero(m)[0])
+                cols.append(nbk[m])
+                vals.append(-oml * s[m])
+            A = sp.csc_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(nh, nh))
+            factors[lc] = spl.splu(A)
+        out[ys, xs, c] = o[ys, xs] + factors[lc].solve(b)
+    return out
