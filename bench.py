@@ -295,6 +295,12 @@ def run_ours(args):
         ctx.set_tuning(ctx.TUNE_PM_VARIANT, args.pm_variant)
     if args.cg_precond is not None:
         ctx.set_tuning(ctx.TUNE_CG_PRECOND, args.cg_precond)
+    if args.pm_bound is not None:
+        ctx.set_tuning(ctx.TUNE_PM_BOUND, args.pm_bound)
+    if args.batch_groups is not None:
+        ctx.set_tuning(ctx.TUNE_BATCH_GROUPS, args.batch_groups)
+    if args.pm_tile is not None:
+        ctx.set_tuning(ctx.TUNE_PM_TILE, args.pm_tile)
     img, mask, p = workload()
     H, W, C = img.shape
     mpix = W * H / 1e6
@@ -626,6 +632,12 @@ def run_case(args):
         ctx.set_tuning(ctx.TUNE_PM_VARIANT, args.pm_variant)
     if args.cg_precond is not None:
         ctx.set_tuning(ctx.TUNE_CG_PRECOND, args.cg_precond)
+    if args.pm_bound is not None:
+        ctx.set_tuning(ctx.TUNE_PM_BOUND, args.pm_bound)
+    if args.batch_groups is not None:
+        ctx.set_tuning(ctx.TUNE_BATCH_GROUPS, args.batch_groups)
+    if args.pm_tile is not None:
+        ctx.set_tuning(ctx.TUNE_PM_TILE, args.pm_tile)
     ctx.set_seed(7)
     img, mask, p = workload()
     if args.case == "batch":
@@ -689,6 +701,14 @@ def main():
     ap.add_argument("--cg-precond", type=int, default=None, choices=[0, 1],
                     help="NL-Poisson CG: 0 plain (the reference's), 1 Jacobi-preconditioned "
                          "(default: the library's, 0)")
+    ap.add_argument("--pm-bound", type=int, default=None, choices=[0, 1],
+                    help="PatchMatch patch-mean lower bound: 1 on, 0 every candidate evaluated "
+                         "(default: the library's, 1)")
+    ap.add_argument("--pm-tile", type=int, default=None,
+                    help="PatchMatch work distribution: 0 static block ranges, n > 0 a device work queue of n "
+                         "target points per grab (default: the library's)")
+    ap.add_argument("--batch-groups", type=int, default=None,
+                    help="concurrent sub-groups of a lockstep batch group (default: the library's, 2)")
     ap.add_argument("--batch-count", type=int, default=64,
                     help="images in the batched-vs-plain comparison (0 skips it)")
     ap.add_argument("--batch-max-side", type=int, default=1024)

@@ -460,6 +460,13 @@ int nli_ctx_set_batch_width(nli_ctx *ctx, int width);
  *                                  sub-group's per-rank tail (its slowest
  *                                  image) overlaps another's work (1..16,
  *                                  default 2).  Identical results.
+ *   NLI_TUNE_PM_TILE               how the persistent PatchMatch kernels
+ *                                  share out the target points: 0 static
+ *                                  ranges (block b takes the b-th contiguous
+ *                                  range); n > 0 a device work queue from
+ *                                  which each warp takes n consecutive points
+ *                                  per atomic grab (1..1024).  Identical
+ *                                  fields.
  * nli_ctx_get_tuning reads them back. */
 #define NLI_TUNE_CG_CLUSTER_CAP 0
 #define NLI_TUNE_CG_UNKNOWNS_PER_CTA 1
@@ -471,6 +478,7 @@ int nli_ctx_set_batch_width(nli_ctx *ctx, int width);
 #define NLI_TUNE_BATCH_MODE 7
 #define NLI_TUNE_PM_BOUND 8
 #define NLI_TUNE_BATCH_GROUPS 9
+#define NLI_TUNE_PM_TILE 10
 int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value);
 int nli_ctx_get_tuning(nli_ctx *ctx, int knob, int *value);
 /* The seed image `index` of a batch runs with. */

@@ -662,6 +662,10 @@ int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value)
 		if (value < 1 || value > 16) return NLI_E_INVALID;
 		ctx->tune_batch_groups = value;
 		return NLI_OK;
+	case NLI_TUNE_PM_TILE:
+		if (value < 0 || value > 1024) return NLI_E_INVALID;
+		ctx->tune_pm_tile = value;
+		return NLI_OK;
 	}
 	return NLI_E_INVALID;
 }
@@ -680,6 +684,7 @@ int nli_ctx_get_tuning(nli_ctx *ctx, int knob, int *value)
 	case NLI_TUNE_BATCH_MODE: *value = ctx->tune_batch_mode; return NLI_OK;
 	case NLI_TUNE_PM_BOUND: *value = ctx->tune_pm_bound; return NLI_OK;
 	case NLI_TUNE_BATCH_GROUPS: *value = ctx->tune_batch_groups; return NLI_OK;
+	case NLI_TUNE_PM_TILE: *value = ctx->tune_pm_tile; return NLI_OK;
 	}
 	return NLI_E_INVALID;
 }

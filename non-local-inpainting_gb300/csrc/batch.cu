@@ -85,12 +85,7 @@ void process_batch_run(nli_ctx *ctx, int n, const nli_process_params *params, co
 	std::vector<int> rcs(n, NLI_OK);
 	auto work = [&](nli_ctx *w) {
 		cudaSetDevice(w->device);
-		w->profiling = ctx->profiling;
-		w->tune_cg_cluster_cap = ctx->tune_cg_cluster_cap;
-		w->tune_cg_unknowns_per_cta = ctx->tune_cg_unknowns_per_cta;
-		w->tune_pm_variant = ctx->tune_pm_variant;
-		w->tune_cg_precond = ctx->tune_cg_precond;
-		w->tune_graph_loop = ctx->tune_graph_loop;
+		w->copy_tuning(*ctx);
 		if (ready) cudaStreamWaitEvent(w->stream, ready, 0);
 		for (;;) {
 			const int k = next.fetch_add(1);

@@ -136,6 +136,7 @@ struct nli_ctx {
 	int tune_batch_mode = 1;             // batches: 1 lockstep (process.cu), 0 worker contexts (batch.cu)
 	int tune_pm_bound = 1;               // PatchMatch: skip candidates by the patch-mean lower bound
 	int tune_batch_groups = 2;           // lockstep: concurrent sub-groups per launch-sharing group
+	int tune_pm_tile = 0;                // PatchMatch: 0 static ranges, n > 0 work queue of n points per grab
 	bool batch_worker = false;           // a worker context of nli_process_batch
 	int max_smem_optin = 0;              // dynamic shared memory per block at most
 	std::vector<nli_ctx *> workers;
@@ -171,6 +172,21 @@ struct nli_ctx {
 	// workspace growth that brings it to 0 fails as an out-of-memory error
 	// without calling cudaMalloc.
 	int fail_alloc_countdown = 0;
+
+	// The launch-shape knobs (nli_ctx_set_tuning) a worker context takes
+	// from its parent.
+	void copy_tuning(const nli_ctx &o)
+	{
+		profiling = o.profiling;
+		tune_cg_cluster_cap = o.tune_cg_cluster_cap;
+		tune_cg_unknowns_per_cta = o.tune_cg_unknowns_per_cta;
+		tune_pm_variant = o.tune_pm_variant;
+		tune_cg_precond = o.tune_cg_precond;
+		tune_graph_loop = o.tune_graph_loop;
+		tune_cg_single_max = o.tune_cg_single_max;
+		tune_pm_bound = o.tune_pm_bound;
+		tune_pm_tile = o.tune_pm_tile;
+	}
 
 	template <class T>
 	T *buf(const std::string &name, size_t count)

@@ -143,6 +143,11 @@ struct PmArgs {
 	// and the largest absolute pixel value of the images (as float bits)
 	const float4 *smom, *tmom;
 	const unsigned *vmax;
+	// device work queue (null: static ranges): the call's counters, one
+	// per launch (init, then each sweep), zeroed before the init launch;
+	// a warp takes `tile` consecutive target points per grab
+	unsigned *queue;
+	int tile;
 };
 
 // Philox key of this PatchMatch call: the seed mixed with the call's index
@@ -158,6 +163,37 @@ template <int KIND>
 struct Kind {
 	static constexpr bool grad = KIND == NLI_DIST_L2_COMBINED || KIND == NLI_DIST_L2_RGBD;
 };
+
+// The work items [0, n) of a persistent PatchMatch launch, visited by the
+// calling warp (f(i) for each of its items, in increasing order).  Without
+// a queue, block b takes the contiguous range [b * chunk, (b + 1) * chunk)
+// and its warps interleave over it, so the warps of an SM work on
+// neighbouring points and share source neighbourhoods in L1.  With a queue
+// (`queue` a counter zeroed before the launch), each warp takes `tile`
+// consecutive items per atomic grab until the list is exhausted, so warps
+// that drew cheap points take more and no SM idles while others finish.
+// Every item's computation is independent of which warp does it and when
+// (the sweeps read the previous field and the random streams are keyed by
+// point), so both give the same field.
+template <class F>
+__device__ __forceinline__ void pm_for_each(int n, unsigned *queue, int tile, F &&f)
+{
+	if (queue) {
+		const int lane = threadIdx.x & 31;
+		for (;;) {
+			unsigned base = 0u;
+			if (lane == 0) base = atomicAdd(queue, (unsigned)tile);
+			base = __shfl_sync(kFull, base, 0);
+			if (base >= (unsigned)n) break;
+			const int stop = min(n, (int)base + tile);
+			for (int i = (int)base; i < stop; i++) f(i);
+		}
+	} else {
+		const int chunk = (n + gridDim.x - 1) / gridDim.x;
+		const int end = min(n, (int)(blockIdx.x + 1) * chunk);
+		for (int i = blockIdx.x * chunk + (threadIdx.x >> 5); i < end; i += blockDim.x >> 5) f(i);
+	}
+}
 
 // A source centre is usable when it is in the source mask and its whole
 // patch lies in the image (the masks of the inpainting driver guarantee the
@@ -737,14 +773,9 @@ __global__ void __launch_bounds__(pm_threads(V), 1) k_pm_init(DistArgs a, PmArgs
 	load_weights(a, m.w);
 	const uint2 key = pm_key(p);
 	unsigned evals = 0, partial = 0;
-	// block b takes the contiguous range [b * chunk, (b + 1) * chunk) of the
-	// raster-ordered target list, its warps interleaved over the range, so
-	// the warps of an SM work on neighbouring points and share source
-	// neighbourhoods in L1
-	const int chunk = (p.nt + gridDim.x - 1) / gridDim.x;
-	const int end = min(p.nt, (int)(blockIdx.x + 1) * chunk);
-	for (int wi = blockIdx.x * chunk + (threadIdx.x >> 5); wi < end; wi += blockDim.x >> 5)
+	pm_for_each(p.nt, p.queue, p.tile, [&](int wi) {
 		pm_init_point<KIND, C, P, V>(p, m, ts, tw, key, p.tlist[wi], init, nnf, dist, evals, partial);
+	});
 	if (lane == 0 && evals) {
 		atomicAdd(counter, (unsigned long long)evals);
 		if (partial) atomicAdd(counter + 1, (unsigned long long)partial);
@@ -856,11 +887,10 @@ __global__ void __launch_bounds__(pm_threads(V), 1) k_pm_sweep(DistArgs a, PmArg
 	int max_shot = -1;
 	// number of random-search windows: max_window, max_window / 2, ..., 1
 	const int windows = 32 - __clz(p.max_window);
-	const int chunk = (p.nt + gridDim.x - 1) / gridDim.x;
-	const int end = min(p.nt, (int)(blockIdx.x + 1) * chunk);
-	for (int wi = blockIdx.x * chunk + (threadIdx.x >> 5); wi < end; wi += blockDim.x >> 5)
+	pm_for_each(p.nt, p.queue ? p.queue + 1 + sweep : nullptr, p.tile, [&](int wi) {
 		pm_sweep_point<KIND, C, P, V>(p, m, ts, tw, key, windows, p.tlist[wi], sweep, jump, nnf_in, dist_in, nnf_out,
 		                              dist_out, evals, partial, improved, max_shot);
+	});
 	if (lane == 0 && evals) {
 		atomicAdd(counter, (unsigned long long)evals);
 		if (partial) atomicAdd(counter + 1, (unsigned long long)partial);
@@ -1056,10 +1086,9 @@ static void sweep_energy(cudaStream_t s, const PmArgs &p, const float *dist, con
 // __grid_constant__ table read through the constant cache, not the L1 data
 // pipe that bounds the sweep).  The persistent kernels see the concatenated
 // target lists of the images still iterating (their `active` flag, written
-// on the device between iterations) as one work list: block b takes the
-// contiguous range [b * chunk, (b + 1) * chunk) of it, its warps interleaved
-// over the range, so an image's points stay together in L1 as in the
-// one-image kernels.
+// on the device between iterations) as one work list, distributed as the
+// one-image kernels distribute theirs (pm_for_each: static block ranges or
+// the device work queue).
 struct PmBatchTask {
 	PmArgs p;
 	int flag;            // index of the image's active flag
@@ -1073,6 +1102,8 @@ struct PmBatchTask {
 struct PmBatchArgs {
 	int n;
 	const int *active;  // per image: still iterating (null: all)
+	unsigned *queue;    // device work queue as PmArgs::queue (null: static ranges)
+	int tile;
 	PmBatchTask t[kBatchMax];
 };
 
@@ -1165,11 +1196,10 @@ __global__ void __launch_bounds__(pm_threads(kPmShared), 1)
 	load_weights(a, m.w);
 	const int total = pm_batch_prefix(B, s_pre);
 	unsigned evals = 0, partial = 0;
-	const int chunk = (total + gridDim.x - 1) / gridDim.x;
-	const int end = min(total, (int)(blockIdx.x + 1) * chunk);
 	int t = 0, tk = -1;
 	uint2 key = make_uint2(0u, 0u);
-	for (int wi = blockIdx.x * chunk + (threadIdx.x >> 5); wi < end; wi += blockDim.x >> 5) {
+	// a warp's items increase, so its image index only moves forward
+	pm_for_each(total, B.queue, B.tile, [&](int wi) {
 		while (wi >= s_pre[t + 1]) t++;
 		const PmBatchTask &T = B.t[t];
 		if (t != tk) {
@@ -1179,7 +1209,7 @@ __global__ void __launch_bounds__(pm_threads(kPmShared), 1)
 		}
 		pm_init_point<KIND, C, P, kPmShared>(T.p, m, ts, tw, key, T.p.tlist[wi - s_pre[t]], T.init, T.nnf_x,
 		                                     T.dist_x, evals, partial);
-	}
+	});
 	if (tk >= 0) pm_batch_count(B.t[tk].counter, counter, evals, partial);
 }
 
@@ -1197,11 +1227,9 @@ __global__ void __launch_bounds__(pm_threads(kPmShared), 1)
 	unsigned evals = 0, partial = 0, improved = 0;
 	int max_shot = -1;
 	const bool even = (sweep % 2) == 0;
-	const int chunk = (total + gridDim.x - 1) / gridDim.x;
-	const int end = min(total, (int)(blockIdx.x + 1) * chunk);
 	int t = 0, tk = -1, windows = 0, jump = 1;
 	uint2 key = make_uint2(0u, 0u);
-	for (int wi = blockIdx.x * chunk + (threadIdx.x >> 5); wi < end; wi += blockDim.x >> 5) {
+	pm_for_each(total, B.queue ? B.queue + 1 + sweep : nullptr, B.tile, [&](int wi) {
 		while (wi >= s_pre[t + 1]) t++;
 		const PmBatchTask &T = B.t[t];
 		if (t != tk) {
@@ -1215,7 +1243,7 @@ __global__ void __launch_bounds__(pm_threads(kPmShared), 1)
 		                                      even ? T.nnf_x : T.nnf_y, even ? T.dist_x : T.dist_y,
 		                                      even ? T.nnf_y : T.nnf_x, even ? T.dist_y : T.dist_x, evals, partial,
 		                                      improved, max_shot);
-	}
+	});
 	if (tk >= 0) pm_batch_count(B.t[tk].counter, counter, evals, partial);
 }
 
@@ -1277,6 +1305,7 @@ void patchmatch_batch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli
 	std::memset(&B, 0, sizeof(B));
 	B.n = n;
 	B.active = active;
+	B.tile = ctx->tune_pm_tile;
 	int maxpix = 0, maxpad = 0, maxnt = 0;
 	for (int i = 0; i < n; i++) {
 		const PmBatchItem &it = items[i];
@@ -1306,6 +1335,8 @@ void patchmatch_batch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli
 		p.calls = it.calls;
 		p.smom = p.tmom = it.mom;
 		p.vmax = it.mom ? it.vmax : nullptr;
+		p.queue = nullptr;  // the launch's queue is B.queue
+		p.tile = 0;
 		T.flag = it.flag;
 		T.counter = it.counter;
 		T.img = it.img;
@@ -1331,6 +1362,11 @@ void patchmatch_batch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli
 	}
 	if (maxnt == 0) return;
 	unsigned long long *counter = ctx->buf<unsigned long long>("pm.counter", 2);
+	if (B.tile > 0) {
+		const int slots = std::max(pm.iterations, 0) + 1;
+		B.queue = ctx->buf<unsigned>("pm.queue", slots);
+		NLI_CUDA(cudaMemsetAsync(B.queue, 0, sizeof(unsigned) * slots, s));
+	}
 	const int taps = a.px * a.py;
 	const size_t smem = pm_smem_bytes(taps, B.t[0].p.rows, B.t[0].p.L, pm_threads(kPmShared) / 32);
 	NLI_REQUIRE(smem <= (size_t)ctx->max_smem_optin, NLI_E_UNSUPPORTED, "PatchMatch shared memory too large");
@@ -1460,6 +1496,13 @@ void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patch
 		p.smom = smom;
 		p.tmom = tmom;
 		p.vmax = vmax;
+		p.queue = nullptr;
+		p.tile = ctx->tune_pm_tile;
+		if (p.tile > 0) {
+			const int slots = std::max(pm.iterations, 0) + 1;
+			p.queue = ctx->buf<unsigned>("pm.queue", slots);
+			NLI_CUDA(cudaMemsetAsync(p.queue, 0, sizeof(unsigned) * slots, s));
+		}
 		if (energy) NLI_CUDA(cudaMemsetAsync(counter, 0, 2 * sizeof(unsigned long long), s));
 		PmMetrics mt;
 		const int iters = std::max(pm.iterations, 0);

@@ -1264,14 +1264,7 @@ void lockstep_batch_run(nli_ctx *ctx, int n, const nli_process_params *params, c
 			nli_ctx *w = ctx->workers[t];
 			try {
 				NLI_CUDA(cudaSetDevice(w->device));
-				w->profiling = ctx->profiling;
-				w->tune_cg_cluster_cap = ctx->tune_cg_cluster_cap;
-				w->tune_cg_unknowns_per_cta = ctx->tune_cg_unknowns_per_cta;
-				w->tune_pm_variant = ctx->tune_pm_variant;
-				w->tune_cg_precond = ctx->tune_cg_precond;
-				w->tune_graph_loop = ctx->tune_graph_loop;
-				w->tune_cg_single_max = ctx->tune_cg_single_max;
-				w->tune_pm_bound = ctx->tune_pm_bound;
+				w->copy_tuning(*ctx);
 				NLI_CUDA(cudaStreamWaitEvent(w->stream, ready, 0));
 				lockstep_group_run(w, sub[t], C, ctx->seed, params, images, masks, widths, heights, outputs,
 				                   stats, host_buffers, rcs, errors);

@@ -98,3 +98,12 @@ def test_tune_batch_mode_and_groups(gpu_ctx):
         assert sorted(res["ms"]) == [1, 3] and gpu_ctx.get_tuning(gpu_ctx.TUNE_BATCH_GROUPS) == res["best"]
     finally:
         autotune.apply(gpu_ctx, batch_mode=1, batch_groups=2)
+
+
+def test_tune_pm_tile(gpu_ctx):
+    from nli_gb300 import autotune
+    case = autotune.patchmatch_case(gpu_ctx, size=160, seed=2)
+    res = autotune.tune_pm_tile(gpu_ctx, case, tiles=(0, 8), repeats=1)
+    assert sorted(res["ms"]) == [0, 8]
+    assert gpu_ctx.get_tuning(gpu_ctx.TUNE_PM_TILE) == res["best"]
+    autotune.apply(gpu_ctx, pm_tile=0)
