@@ -301,6 +301,8 @@ def run_ours(args):
         ctx.set_tuning(ctx.TUNE_BATCH_GROUPS, args.batch_groups)
     if args.pm_tile is not None:
         ctx.set_tuning(ctx.TUNE_PM_TILE, args.pm_tile)
+    if args.graph_loop is not None:
+        ctx.set_tuning(ctx.TUNE_GRAPH_LOOP, args.graph_loop)
     img, mask, p = workload()
     H, W, C = img.shape
     mpix = W * H / 1e6
@@ -496,17 +498,18 @@ def hole_psnr(out, truth, mask):
     return float("inf") if mse == 0 else 10.0 * np.log10(255.0 ** 2 / mse)
 
 
-def batch_reference_gaps(items5, outs):
+def batch_reference_gaps(items5, outs, batch=(5, 64, 1024)):
     """Hole PSNR against the truth (the input's hole pixels) of our outputs
     and of the reference's (tests/golden/batch_reference_*.npz, made by
     tests/golden/make_golden.py --batch) for the batch items that have
-    one; gap = ours - reference (dB)."""
+    one; gap = ours - reference (dB).  batch = (seed, count, largest side)
+    of the batch `items5` is: only references of that batch compare."""
     import glob
     rows = []
     for path in sorted(glob.glob(os.path.join(GOLDEN, "batch_reference_*.npz"))):
         g = np.load(path)
         i = int(g["index"])
-        if i >= len(outs) or tuple(g["batch"]) != (5, 64, 1024):
+        if i >= len(outs) or tuple(int(v) for v in g["batch"]) != tuple(batch):
             continue
         img, mask = items5[i][0], items5[i][1]
         truth = img[mask > 0].astype(np.float64)
@@ -601,7 +604,7 @@ def batch_compare(pkg, ctx, args, local):
 
     kb, kp = (kernel_ms(batched), kernel_ms(plain)) if args.batch_profile else (None, None)
     host = [o.cpu().numpy() for o in ref]
-    gaps = batch_reference_gaps(items5, host)
+    gaps = batch_reference_gaps(items5, host, (5, args.batch_count, args.batch_max_side))
     return {"workload": "uneven batch: %d images, sides log-uniform 128-%d, aspect 0.5-2, 5-30%% ellipse/stroke "
                         "holes, nlmeans/nlpoisson alternating, patch 9, scales |round(log(0.1 size)/log(0.75))|, "
                         "automatic coarsest rate (seed 5)" % (len(items), args.batch_max_side),
@@ -638,6 +641,8 @@ def run_case(args):
         ctx.set_tuning(ctx.TUNE_BATCH_GROUPS, args.batch_groups)
     if args.pm_tile is not None:
         ctx.set_tuning(ctx.TUNE_PM_TILE, args.pm_tile)
+    if args.graph_loop is not None:
+        ctx.set_tuning(ctx.TUNE_GRAPH_LOOP, args.graph_loop)
     ctx.set_seed(7)
     img, mask, p = workload()
     if args.case == "batch":
@@ -701,12 +706,16 @@ def main():
     ap.add_argument("--cg-precond", type=int, default=None, choices=[0, 1],
                     help="NL-Poisson CG: 0 plain (the reference's), 1 Jacobi-preconditioned "
                          "(default: the library's, 0)")
-    ap.add_argument("--pm-bound", type=int, default=None, choices=[0, 1],
-                    help="PatchMatch patch-mean lower bound: 1 on, 0 every candidate evaluated "
-                         "(default: the library's, 1)")
+    ap.add_argument("--pm-bound", type=int, default=None, choices=[0, 1, 2],
+                    help="PatchMatch lower bound: 2 patch means and deviations, 1 means, 0 every candidate "
+                         "evaluated (default: the library's, 2)")
     ap.add_argument("--pm-tile", type=int, default=None,
                     help="PatchMatch work distribution: 0 static block ranges, n > 0 a device work queue of n "
-                         "target points per grab (default: the library's)")
+                         "target points per grab (default: the library's, 1)")
+    ap.add_argument("--graph-loop", type=int, default=None, choices=[0, 1, 2],
+                    help="iteration loops as CUDA graphs: 1 plain runs and lockstep batches, 2 also worker "
+                         "batches, 0 host loops (for profilers that cannot see into conditional graphs); "
+                         "default: the library's, 1")
     ap.add_argument("--batch-groups", type=int, default=None,
                     help="concurrent sub-groups of a lockstep batch group (default: the library's, 2)")
     ap.add_argument("--batch-count", type=int, default=64,

@@ -443,15 +443,19 @@ int nli_ctx_set_batch_width(nli_ctx *ctx, int width);
  *                                  one CUDA graph; 0 worker contexts -- up to
  *                                  the batch width of whole nli_process runs
  *                                  on their own streams.  Identical results.
- *   NLI_TUNE_PM_BOUND              1 (default): PatchMatch skips a candidate
- *                                  whose patch means (of the image and its
- *                                  forward differences, weighted by the patch
+ *   NLI_TUNE_PM_BOUND              PatchMatch skips a candidate whose patch
+ *                                  statistics (of the image and its forward
+ *                                  differences, weighted by the patch
  *                                  weights) differ from the target's by
- *                                  enough that, by Jensen's inequality, its
- *                                  distance cannot beat the current match;
- *                                  0: every candidate is evaluated.  The
- *                                  bound keeps a rounding margin, so fields
- *                                  and distances are identical either way.
+ *                                  enough that its distance provably cannot
+ *                                  beat the current match: 2 (default) by
+ *                                  the weighted means and standard
+ *                                  deviations (L2 kinds; L1 uses the means),
+ *                                  1 by the means alone (Jensen's
+ *                                  inequality), 0 every candidate is
+ *                                  evaluated.  The bound keeps a rounding
+ *                                  margin, so fields and distances are
+ *                                  identical in all three.
  *   NLI_TUNE_BATCH_GROUPS          lockstep batches: the images of one
  *                                  launch-sharing group are dealt (largest
  *                                  first, to the least-loaded) into this many
@@ -459,14 +463,14 @@ int nli_ctx_set_batch_width(nli_ctx *ctx, int width);
  *                                  own streams and workspaces, so one
  *                                  sub-group's per-rank tail (its slowest
  *                                  image) overlaps another's work (1..16,
- *                                  default 2).  Identical results.
+ *                                  default 4).  Identical results.
  *   NLI_TUNE_PM_TILE               how the persistent PatchMatch kernels
- *                                  share out the target points: 0 static
+ *                                  share out the target points: n > 0 a
+ *                                  device work queue from which each warp
+ *                                  takes n consecutive points per atomic
+ *                                  grab (1..1024, default 1); 0 static
  *                                  ranges (block b takes the b-th contiguous
- *                                  range); n > 0 a device work queue from
- *                                  which each warp takes n consecutive points
- *                                  per atomic grab (1..1024).  Identical
- *                                  fields.
+ *                                  range).  Identical fields.
  * nli_ctx_get_tuning reads them back. */
 #define NLI_TUNE_CG_CLUSTER_CAP 0
 #define NLI_TUNE_CG_UNKNOWNS_PER_CTA 1

@@ -158,12 +158,13 @@ def tune_cg_single(ctx, cases=None, limits=(0, 512, 1024, 2048, 4096), repeats=3
 
 
 def tune_pm_bound(ctx, case=None, repeats=3, seed=0):
-    """Times one PatchMatch call with and without the lower-bound test and
-    keeps the faster.  Returns {"best": 0 or 1, "ms": {0: ms, 1: ms}}."""
+    """Times one PatchMatch call per lower-bound mode (0 none, 1 patch
+    means, 2 means and deviations) and keeps the fastest.  Returns
+    {"best": mode, "ms": {mode: ms}}."""
     import torch
     dist, pm, u, src, tgt = case if case is not None else patchmatch_case(ctx)
     times = {}
-    for v in (0, 1):
+    for v in (0, 1, 2):
         ctx.set_tuning(ctx.TUNE_PM_BOUND, v)
         ctx.set_seed(seed)
         ctx.patchmatch(dist, pm, u, src, u, tgt, want_energy=False)  # warm

@@ -655,7 +655,7 @@ int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value)
 		ctx->tune_batch_mode = value;
 		return NLI_OK;
 	case NLI_TUNE_PM_BOUND:
-		if (value != 0 && value != 1) return NLI_E_INVALID;
+		if (value < 0 || value > 2) return NLI_E_INVALID;
 		ctx->tune_pm_bound = value;
 		return NLI_OK;
 	case NLI_TUNE_BATCH_GROUPS:

@@ -143,6 +143,9 @@ struct PmArgs {
 	// and the largest absolute pixel value of the images (as float bits)
 	const float4 *smom, *tmom;
 	const unsigned *vmax;
+	// 1: the tables also hold the weighted standard deviations (of the
+	// image and of its forward differences), and the bound uses them
+	int dev;
 	// device work queue (null: static ranges): the call's counters, one
 	// per launch (init, then each sweep), zeroed before the init launch;
 	// a warp takes `tile` consecutive target points per grab
@@ -386,6 +389,25 @@ __device__ __forceinline__ float combine(const Acc &A, const PmArgs &p)
 	return v;
 }
 
+// float4 helpers of the patch statistics
+__device__ __forceinline__ float4 f4_fma(float w, float4 v, float4 a)
+{
+	return make_float4(fmaf(w, v.x, a.x), fmaf(w, v.y, a.y), fmaf(w, v.z, a.z), fmaf(w, v.w, a.w));
+}
+__device__ __forceinline__ float4 f4_sub(float4 a, float4 b)
+{
+	return make_float4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w);
+}
+__device__ __forceinline__ float4 f4_wsq(float w, float4 d, float4 a)
+{
+	return make_float4(fmaf(w, d.x * d.x, a.x), fmaf(w, d.y * d.y, a.y), fmaf(w, d.z * d.z, a.z),
+	                   fmaf(w, d.w * d.w, a.w));
+}
+__device__ __forceinline__ float4 f4_sqrt(float4 a)
+{
+	return make_float4(sqrtf(a.x), sqrtf(a.y), sqrtf(a.z), sqrtf(a.w));
+}
+
 // ------------------------------------------------ patch-mean lower bound
 // Jensen's inequality gives, for weights v_k >= 0 summing to V,
 //   sum_k v_k |d_k|^2 >= |sum_k v_k d_k|^2 / V,   sum_k v_k |d_k|_1 >= |sum_k v_k d_k|_1.
@@ -394,12 +416,25 @@ __device__ __forceinline__ float combine(const Acc &A, const PmArgs &p)
 // two patches' weighted means of the image or of its forward differences;
 // the mean of the differences is the difference of means one column (row)
 // apart.  So a candidate whose patch means differ enough from the target's
-// cannot beat the current match and is not evaluated.  Exactness: every
-// mean difference is shrunk by a slack (2e-4 of the largest pixel value)
-// that covers the float rounding of the means and of the kernel's per-tap
-// differences, and the bound must exceed the current distance by a 1e-4
-// relative margin that covers the rounding of the kernel's sums; the field
-// and distances are those of evaluating every candidate.
+// cannot beat the current match and is not evaluated.
+//
+// With the weighted standard deviations as well (PmArgs::dev, the L2
+// kinds), the bound is tighter: for weights summing to 1,
+//   sum_k w_k d_k^2 = (sum_k w_k d_k)^2 + sum_k w_k (d_k - mean d)^2,
+// and with d = s - t the centred part is the squared weighted L2 distance of
+// the centred patches, at least (sigma_s - sigma_t)^2 by the reverse
+// triangle inequality.  So each channel's colour term is bounded by the
+// squared mean difference plus the squared difference of standard
+// deviations, and each gradient term likewise with the deviations of the
+// forward differences.
+//
+// Exactness: every mean and deviation difference is shrunk by a slack (2e-4
+// of the largest pixel value) that covers the float rounding of the tables
+// (sums of 81 products: a few 1e-6 of the largest value) and of the
+// kernel's per-tap differences, and the bound must exceed the current
+// distance by a 1e-4 relative margin that covers the rounding of the
+// kernel's sums; the field and distances are those of evaluating every
+// candidate.
 __device__ __forceinline__ float shrink(float v, float slack) { return fmaxf(fabsf(v) - slack, 0.f); }
 
 // True when candidate (cx, cy) for target (x, y) provably cannot reach a
@@ -409,35 +444,39 @@ template <int KIND, int C>
 __device__ __forceinline__ bool bound_rejects(const PmArgs &p, int x, int y, int cx, int cy, float bd)
 {
 	const float4 *M = p.smom + (size_t)cy * p.sWp + cx;
-	const float4 m0 = __ldg(M), mx = __ldg(M + 1), my = __ldg(M + p.sWp);
 	const float4 *T = p.tmom + (size_t)y * p.tWp + x;
-	const float4 t0 = __ldg(T), txx = __ldg(T + 1), tyy = __ldg(T + p.tWp);
 	const float slack = 2e-4f * __uint_as_float(__ldg(p.vmax));
-	const float mc[4] = {m0.x, m0.y, m0.z, m0.w}, tc[4] = {t0.x, t0.y, t0.z, t0.w};
-	const float sx[4] = {mx.x - m0.x, mx.y - m0.y, mx.z - m0.z, mx.w - m0.w};
-	const float sy[4] = {my.x - m0.x, my.y - m0.y, my.z - m0.z, my.w - m0.w};
-	const float tx[4] = {txx.x - t0.x, txx.y - t0.y, txx.z - t0.z, txx.w - t0.w};
-	const float ty[4] = {tyy.x - t0.x, tyy.y - t0.y, tyy.z - t0.z, tyy.w - t0.w};
+	// per-channel terms, the depth channel of L2 RGBD kept apart; each
+	// statistic is read, folded in and dropped in turn (few live registers)
 	float col = 0.f, grad = 0.f, dcol = 0.f, dgrad = 0.f;
+	auto add = [&](float4 d, bool g) {
+		const float v[4] = {d.x, d.y, d.z, d.w};
 #pragma unroll
-	for (int c = 0; c < C; c++) {
-		const float dc = shrink(mc[c] - tc[c], slack);
-		const bool depth = KIND == NLI_DIST_L2_RGBD && c == 3;
-		if (KIND == NLI_DIST_L1_NORM) {
-			col += dc;
-			continue;
-		}
-		if (depth)
-			dcol = dc * dc;
-		else
-			col = fmaf(dc, dc, col);
-		if (Kind<KIND>::grad) {
-			const float gx = shrink(sx[c] - tx[c], slack), gy = shrink(sy[c] - ty[c], slack);
-			const float g = fmaf(gx, gx, gy * gy);
-			if (depth)
-				dgrad = g;
+		for (int c = 0; c < C; c++) {
+			const float e = shrink(v[c], slack);
+			const bool depth = KIND == NLI_DIST_L2_RGBD && c == 3;
+			if (KIND == NLI_DIST_L1_NORM)
+				col += e;
+			else if (depth)
+				(g ? dgrad : dcol) += e * e;
 			else
-				grad += g;
+				(g ? grad : col) += e * e;
+		}
+	};
+	const float4 m0 = __ldg(M), t0 = __ldg(T);
+	add(f4_sub(m0, t0), false);
+	if (Kind<KIND>::grad) {
+		// the mean of the forward differences: means one column (row) apart
+		add(f4_sub(f4_sub(__ldg(M + 1), m0), f4_sub(__ldg(T + 1), t0)), true);
+		add(f4_sub(f4_sub(__ldg(M + p.sWp), m0), f4_sub(__ldg(T + p.tWp), t0)), true);
+	}
+	if (KIND != NLI_DIST_L1_NORM && p.dev) {
+		// weighted standard deviations: of the image, of its x and y differences
+		const size_t sn = (size_t)p.sWp * (p.sH + 1), tn = (size_t)p.tWp * (p.tH + 1);
+		add(f4_sub(__ldg(M + sn), __ldg(T + tn)), false);
+		if (Kind<KIND>::grad) {
+			add(f4_sub(__ldg(M + 2 * sn), __ldg(T + 2 * tn)), true);
+			add(f4_sub(__ldg(M + 3 * sn), __ldg(T + 3 * tn)), true);
 		}
 	}
 	float lb = col;
@@ -447,30 +486,56 @@ __device__ __forceinline__ bool bound_rejects(const PmArgs &p, int x, int y, int
 	return lb * (1.0f - 1e-4f) >= bd * P;
 }
 
-// Weighted patch means of the padded image at every position of the
-// (W + 1) x (H + 1) grid (window clamped to the grid), and the largest
-// absolute pixel value (atomicMax on the float bits of non-negative values).
+// Weighted patch statistics of the padded image at every position of the
+// (W + 1) x (H + 1) grid (window clamped to the grid): table 0 the weighted
+// means; with `dev`, tables 1-3 (each n = (W + 1)(H + 1) float4 further) the
+// weighted standard deviations of the image and of its forward differences
+// in x and in y, sqrt(sum_k w_k (v_k - mean)^2), from a second, centred
+// pass.  Also the largest absolute pixel value (atomicMax on the float bits
+// of non-negative values).
 __device__ __forceinline__ void moments_span(const DistArgs &a, const float4 *__restrict__ pad, int W, int H,
-                                             float4 *__restrict__ mom, unsigned *vmax, int first, int stride)
+                                             float4 *__restrict__ mom, unsigned *vmax, int first, int stride,
+                                             bool dev)
 {
 	const int Wp = W + 1, n = Wp * (H + 1);
 	float vm = 0.f;
+	const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
 	for (int i = first; i < n; i += stride) {
 		const int y = i / Wp, x = i - y * Wp;
-		float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+		float4 acc = zero, ax = zero, ay = zero;
 		for (int dy = 0; dy < a.py; dy++) {
 			const int yy = min(max(y - a.ry + dy, 0), H);
+			const float4 *row = pad + (size_t)yy * Wp, *below = pad + (size_t)min(yy + 1, H) * Wp;
 			for (int dx = 0; dx < a.px; dx++) {
 				const int xx = min(max(x - a.rx + dx, 0), W);
-				const float4 v = __ldg(pad + (size_t)yy * Wp + xx);
+				const float4 v = __ldg(row + xx);
 				const float w = a.weights[dy * a.px + dx];
-				acc.x = fmaf(w, v.x, acc.x);
-				acc.y = fmaf(w, v.y, acc.y);
-				acc.z = fmaf(w, v.z, acc.z);
-				acc.w = fmaf(w, v.w, acc.w);
+				acc = f4_fma(w, v, acc);
+				if (dev) {
+					ax = f4_fma(w, f4_sub(__ldg(row + min(xx + 1, W)), v), ax);
+					ay = f4_fma(w, f4_sub(__ldg(below + xx), v), ay);
+				}
 			}
 		}
 		mom[i] = acc;
+		if (dev) {
+			float4 s = zero, sx = zero, sy = zero;
+			for (int dy = 0; dy < a.py; dy++) {
+				const int yy = min(max(y - a.ry + dy, 0), H);
+				const float4 *row = pad + (size_t)yy * Wp, *below = pad + (size_t)min(yy + 1, H) * Wp;
+				for (int dx = 0; dx < a.px; dx++) {
+					const int xx = min(max(x - a.rx + dx, 0), W);
+					const float4 v = __ldg(row + xx);
+					const float w = a.weights[dy * a.px + dx];
+					s = f4_wsq(w, f4_sub(v, acc), s);
+					sx = f4_wsq(w, f4_sub(f4_sub(__ldg(row + min(xx + 1, W)), v), ax), sx);
+					sy = f4_wsq(w, f4_sub(f4_sub(__ldg(below + xx), v), ay), sy);
+				}
+			}
+			mom[(size_t)n + i] = f4_sqrt(s);
+			mom[2 * (size_t)n + i] = f4_sqrt(sx);
+			mom[3 * (size_t)n + i] = f4_sqrt(sy);
+		}
 		const float4 v = __ldg(pad + i);
 		vm = fmaxf(vm, fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w))));
 	}
@@ -479,9 +544,9 @@ __device__ __forceinline__ void moments_span(const DistArgs &a, const float4 *__
 }
 
 __global__ void k_pm_moments(DistArgs a, const float4 *__restrict__ pad, int W, int H, float4 *__restrict__ mom,
-                             unsigned *vmax)
+                             unsigned *vmax, int dev)
 {
-	moments_span(a, pad, W, H, mom, vmax, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+	moments_span(a, pad, W, H, mom, vmax, blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, dev != 0);
 }
 
 // Evaluates the n candidates held one per lane (packed x | y << 16, lane i
@@ -1168,7 +1233,7 @@ __global__ void k_pm_moments_batch(DistArgs a, const __grid_constant__ PmBatchAr
 	const PmBatchTask &T = B.t[t];
 	if (!batch_on(B.active, T.flag) || !T.p.smom) return;
 	moments_span(a, T.p.src, T.p.sW, T.p.sH, const_cast<float4 *>(T.p.smom), const_cast<unsigned *>(T.p.vmax),
-	             blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x);
+	             blockIdx.x * blockDim.x + threadIdx.x, gridDim.x * blockDim.x, T.p.dev != 0);
 }
 
 // k_fill_nnf per active image: the result field to "none", and the image's
@@ -1335,6 +1400,8 @@ void patchmatch_batch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli
 		p.calls = it.calls;
 		p.smom = p.tmom = it.mom;
 		p.vmax = it.mom ? it.vmax : nullptr;
+		// the item's table holds room for the deviations (4 tables)
+		p.dev = (it.mom && ctx->tune_pm_bound == 2 && dp.kind != NLI_DIST_L1_NORM) ? 1 : 0;
 		p.queue = nullptr;  // the launch's queue is B.queue
 		p.tile = 0;
 		T.flag = it.flag;
@@ -1426,20 +1493,22 @@ void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patch
 	// patch means for the lower bound (NLI_TUNE_PM_BOUND)
 	float4 *smom = nullptr, *tmom = nullptr;
 	unsigned *vmax = nullptr;
+	// the deviation tables serve the L2 kinds (NLI_TUNE_PM_BOUND 2)
+	const int dev = (ctx->tune_pm_bound == 2 && dp.kind != NLI_DIST_L1_NORM) ? 1 : 0;
 	if (ctx->tune_pm_bound) {
 		DistArgs da;
 		fill_dist_args(da, dp, C);
 		vmax = ctx->buf<unsigned>("pm.vmax", 1);
 		NLI_CUDA(cudaMemsetAsync(vmax, 0, sizeof(unsigned), s));
-		smom = ctx->buf<float4>("pm.smom", (size_t)(sW + 1) * (sH + 1));
 		const int ns = (sW + 1) * (sH + 1);
-		k_pm_moments<<<(ns + 255) / 256, 256, 0, s>>>(da, s4, sW, sH, smom, vmax);
+		smom = ctx->buf<float4>("pm.smom", (size_t)ns * (dev ? 4 : 1));
+		k_pm_moments<<<(ns + 255) / 256, 256, 0, s>>>(da, s4, sW, sH, smom, vmax, dev);
 		NLI_CHECK_LAUNCH();
 		tmom = smom;
 		if (t4 != s4) {
-			tmom = ctx->buf<float4>("pm.tmom", (size_t)(tW + 1) * (tH + 1));
 			const int nt4 = (tW + 1) * (tH + 1);
-			k_pm_moments<<<(nt4 + 255) / 256, 256, 0, s>>>(da, t4, tW, tH, tmom, vmax);
+			tmom = ctx->buf<float4>("pm.tmom", (size_t)nt4 * (dev ? 4 : 1));
+			k_pm_moments<<<(nt4 + 255) / 256, 256, 0, s>>>(da, t4, tW, tH, tmom, vmax, dev);
 			NLI_CHECK_LAUNCH();
 		}
 	}
@@ -1496,6 +1565,7 @@ void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patch
 		p.smom = smom;
 		p.tmom = tmom;
 		p.vmax = vmax;
+		p.dev = smom ? dev : 0;
 		p.queue = nullptr;
 		p.tile = ctx->tune_pm_tile;
 		if (p.tile > 0) {

@@ -685,7 +685,8 @@ class Lockstep {
 			m.scaled = a.take<int32_t>(2 * n0);
 			m.nnf_y = a.take<int32_t>(2 * n0);
 			m.pad = a.take<float4>((size_t)(m.W + 1) * (m.H + 1));
-			m.mom = a.take<float4>((size_t)(m.W + 1) * (m.H + 1));
+			// patch means and deviations of the PatchMatch bound (4 tables)
+			m.mom = a.take<float4>((size_t)(m.W + 1) * (m.H + 1) * 4);
 			m.dist_x = a.take<float>(n0);
 			m.dist_y = a.take<float>(n0);
 			m.vmax = a.take<unsigned>(1);

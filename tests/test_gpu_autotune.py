@@ -74,9 +74,9 @@ def test_tune_cg_single_and_pm_bound(gpu_ctx):
     assert gpu_ctx.get_tuning(gpu_ctx.TUNE_CG_SINGLE_MAX) == res["best"]
     case = autotune.patchmatch_case(gpu_ctx, size=160, seed=2)
     res = autotune.tune_pm_bound(gpu_ctx, case, repeats=1)
-    assert sorted(res["ms"]) == [0, 1]
+    assert sorted(res["ms"]) == [0, 1, 2]
     assert gpu_ctx.get_tuning(gpu_ctx.TUNE_PM_BOUND) == res["best"]
-    autotune.apply(gpu_ctx, cg_single=1024, pm_bound=1)
+    autotune.apply(gpu_ctx, cg_single=1024, pm_bound=2)
 
 
 def test_tune_batch_mode_and_groups(gpu_ctx):
@@ -97,7 +97,7 @@ def test_tune_batch_mode_and_groups(gpu_ctx):
         res = autotune.tune_batch_groups(gpu_ctx, items, params, groups=(1, 3))
         assert sorted(res["ms"]) == [1, 3] and gpu_ctx.get_tuning(gpu_ctx.TUNE_BATCH_GROUPS) == res["best"]
     finally:
-        autotune.apply(gpu_ctx, batch_mode=1, batch_groups=2)
+        autotune.apply(gpu_ctx, batch_mode=1, batch_groups=4)
 
 
 def test_tune_pm_tile(gpu_ctx):
@@ -106,4 +106,4 @@ def test_tune_pm_tile(gpu_ctx):
     res = autotune.tune_pm_tile(gpu_ctx, case, tiles=(0, 8), repeats=1)
     assert sorted(res["ms"]) == [0, 8]
     assert gpu_ctx.get_tuning(gpu_ctx.TUNE_PM_TILE) == res["best"]
-    autotune.apply(gpu_ctx, pm_tile=0)
+    autotune.apply(gpu_ctx, pm_tile=1)

@@ -187,7 +187,7 @@ def test_lockstep_concurrent_groups(gpu_ctx, groups):
         gpu_ctx.set_seed(61)
         dev, _ = gpu_ctx.process_batch_device(items, params)
     finally:
-        gpu_ctx.set_tuning(gpu_ctx.TUNE_BATCH_GROUPS, 2)
+        gpu_ctx.set_tuning(gpu_ctx.TUNE_BATCH_GROUPS, 4)
     for i in range(len(items)):
         assert np.array_equal(got[i], want[i]), i
         assert np.array_equal(dev[i].cpu().numpy(), want[i]), i

@@ -1,11 +1,13 @@
-"""The patch-mean lower bound of PatchMatch (NLI_TUNE_PM_BOUND): a candidate
-whose weighted patch means differ enough from the target's is not
-evaluated, because by Jensen's inequality it cannot beat the current match.
-The bound keeps a rounding margin, so the fields and distances must be bit
-for bit those of evaluating every candidate -- for every distance kind and
-channel count, patch sizes with and without compiled rows, separate source
-and target images, other patch weights, and whole runs (plain and batched)
--- while fewer candidates are evaluated."""
+"""The lower bounds of PatchMatch (NLI_TUNE_PM_BOUND): a candidate whose
+weighted patch means (1), or means and standard deviations (2, the
+default), differ enough from the target's is not evaluated, because it
+provably cannot beat the current match.  The bounds keep a rounding
+margin, so the fields and distances must be bit for bit those of
+evaluating every candidate -- for every distance kind and channel count,
+patch sizes with and without compiled rows, separate source and target
+images, other patch weights, and whole runs (plain and batched) -- while
+fewer candidates are evaluated, and fewer with the deviations than with
+the means alone."""
 import numpy as np
 import pytest
 
@@ -34,15 +36,17 @@ def scene(C, seed, w, h, r):
 
 
 def both(ctx, fn):
+    """(result, candidates evaluated) with the bound off, by means, by
+    means and deviations."""
     out = []
-    for b in (0, 1):
+    for b in (0, 1, 2):
         ctx.set_tuning(ctx.TUNE_PM_BOUND, b)
         try:
             c0 = ctx.counters()["candidates"]
             r = fn()
             out.append((r, ctx.counters()["candidates"] - c0))
         finally:
-            ctx.set_tuning(ctx.TUNE_PM_BOUND, 1)
+            ctx.set_tuning(ctx.TUNE_PM_BOUND, 2)
     return out
 
 
@@ -62,10 +66,11 @@ def test_bound_keeps_fields(gpu_ctx, kind, C, P, sigma):
         nnf2, dist2, _ = gpu_ctx.patchmatch(d, pm, img, s, img, t, init=nnf)  # a warm start, as the driver's
         return npy(nnf), npy(dist), e, npy(nnf2), npy(dist2)
 
-    (off, n_off), (on, n_on) = both(gpu_ctx, one)
-    for a, b in zip(off, on):
+    (off, n_off), (on, n_on), (dv, n_dv) = both(gpu_ctx, one)
+    for a, b, c in zip(off, on, dv):
         assert np.array_equal(np.asarray(a), np.asarray(b))
-    assert n_on <= n_off
+        assert np.array_equal(np.asarray(a), np.asarray(c))
+    assert n_dv <= n_on <= n_off
 
 
 def test_bound_separate_source_and_target(gpu_ctx):
@@ -86,10 +91,11 @@ def test_bound_separate_source_and_target(gpu_ctx):
         nnf, dist, e = gpu_ctx.patchmatch(d, pm, src, smask, tgt, tmask)
         return npy(nnf), npy(dist), e
 
-    (off, n_off), (on, n_on) = both(gpu_ctx, one)
-    for a, b in zip(off, on):
+    (off, n_off), (on, n_on), (dv, n_dv) = both(gpu_ctx, one)
+    for a, b, c in zip(off, on, dv):
         assert np.array_equal(np.asarray(a), np.asarray(b))
-    assert n_on < n_off
+        assert np.array_equal(np.asarray(a), np.asarray(c))
+    assert n_dv <= n_on < n_off
 
 
 def test_bound_whole_runs(gpu_ctx):
@@ -107,11 +113,13 @@ def test_bound_whole_runs(gpu_ctx):
         outs.append(gpu_ctx.process_batch(items, params))
         return outs
 
-    (off, n_off), (on, n_on) = both(gpu_ctx, runs)
-    for (o1, s1), (o2, s2) in zip(off[:-1], on[:-1]):
-        assert np.array_equal(o1, o2)
-        assert s1["iterations"] == s2["iterations"] and s1["last_difference"] == s2["last_difference"]
-    for o1, o2 in zip(off[-1][0], on[-1][0]):
-        assert np.array_equal(o1, o2)
-    assert n_on < n_off
-    print("candidates evaluated: %d without the bound, %d with it (%.1f %%)" % (n_off, n_on, 100.0 * n_on / n_off))
+    (off, n_off), (on, n_on), (dv, n_dv) = both(gpu_ctx, runs)
+    for other in (on, dv):
+        for (o1, s1), (o2, s2) in zip(off[:-1], other[:-1]):
+            assert np.array_equal(o1, o2)
+            assert s1["iterations"] == s2["iterations"] and s1["last_difference"] == s2["last_difference"]
+        for o1, o2 in zip(off[-1][0], other[-1][0]):
+            assert np.array_equal(o1, o2)
+    assert n_dv < n_on < n_off
+    print("candidates evaluated: %d without a bound, %d with the means (%.1f %%), %d with means and deviations "
+          "(%.1f %%)" % (n_off, n_on, 100.0 * n_on / n_off, n_dv, 100.0 * n_dv / n_off))

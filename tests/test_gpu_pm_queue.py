@@ -13,7 +13,7 @@ from nli_gb300 import _abi
 
 pytestmark = pytest.mark.gpu
 
-TILES = (1, 3, 8, 64, 1024)
+TILES = (1, 3, 8, 64, 1024)  # 0 (static ranges) is the comparison
 
 
 def npy(t):
@@ -39,7 +39,7 @@ def per_tile(ctx, fn, tiles=(0,) + TILES):
             c1 = ctx.counters()
             out[t] = (r, c1["candidates"] - c0["candidates"], c1["candidates_partial"] - c0["candidates_partial"])
         finally:
-            ctx.set_tuning(ctx.TUNE_PM_TILE, 0)
+            ctx.set_tuning(ctx.TUNE_PM_TILE, 1)
     return out
 
 
@@ -92,7 +92,7 @@ def test_queue_whole_runs_plain_and_lockstep(gpu_ctx):
         batch, _ = gpu_ctx.process_batch(items, params)
         return plain, batch
 
-    res = per_tile(gpu_ctx, runs, tiles=(0, 4, 32))
+    res = per_tile(gpu_ctx, runs, tiles=(0, 1, 4, 32))
     (plain0, batch0), _, _ = res[0]
     for i in range(len(items)):
         assert np.array_equal(batch0[i], plain0[i]), i
@@ -109,4 +109,4 @@ def test_tile_knob_validates(gpu_ctx):
             gpu_ctx.set_tuning(gpu_ctx.TUNE_PM_TILE, bad)
     gpu_ctx.set_tuning(gpu_ctx.TUNE_PM_TILE, 1024)
     assert gpu_ctx.get_tuning(gpu_ctx.TUNE_PM_TILE) == 1024
-    gpu_ctx.set_tuning(gpu_ctx.TUNE_PM_TILE, 0)
+    gpu_ctx.set_tuning(gpu_ctx.TUNE_PM_TILE, 1)
