@@ -471,6 +471,13 @@ int nli_ctx_set_batch_width(nli_ctx *ctx, int width);
  *                                  grab (1..1024, default 1); 0 static
  *                                  ranges (block b takes the b-th contiguous
  *                                  range).  Identical fields.
+ *   NLI_TUNE_PM_CHECK              PatchMatch kernels of compiled patch
+ *                                  sizes (9x9): bit r set = after window row
+ *                                  r, a step of candidates stops when every
+ *                                  partial sum has reached the current
+ *                                  distance (exact: the terms are
+ *                                  non-negative); 0 (default) one test after
+ *                                  rows / 2 - 1 rows.  Identical fields.
  * nli_ctx_get_tuning reads them back. */
 #define NLI_TUNE_CG_CLUSTER_CAP 0
 #define NLI_TUNE_CG_UNKNOWNS_PER_CTA 1
@@ -483,6 +490,7 @@ int nli_ctx_set_batch_width(nli_ctx *ctx, int width);
 #define NLI_TUNE_PM_BOUND 8
 #define NLI_TUNE_BATCH_GROUPS 9
 #define NLI_TUNE_PM_TILE 10
+#define NLI_TUNE_PM_CHECK 11
 int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value);
 int nli_ctx_get_tuning(nli_ctx *ctx, int knob, int *value);
 /* The seed image `index` of a batch runs with. */
