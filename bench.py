@@ -303,8 +303,6 @@ def run_ours(args):
         ctx.set_tuning(ctx.TUNE_PM_TILE, args.pm_tile)
     if args.graph_loop is not None:
         ctx.set_tuning(ctx.TUNE_GRAPH_LOOP, args.graph_loop)
-    if args.pm_check is not None:
-        ctx.set_tuning(ctx.TUNE_PM_CHECK, args.pm_check)
     img, mask, p = workload()
     H, W, C = img.shape
     mpix = W * H / 1e6
@@ -645,8 +643,6 @@ def run_case(args):
         ctx.set_tuning(ctx.TUNE_PM_TILE, args.pm_tile)
     if args.graph_loop is not None:
         ctx.set_tuning(ctx.TUNE_GRAPH_LOOP, args.graph_loop)
-    if args.pm_check is not None:
-        ctx.set_tuning(ctx.TUNE_PM_CHECK, args.pm_check)
     ctx.set_seed(7)
     img, mask, p = workload()
     if args.case == "batch":
@@ -711,14 +707,11 @@ def main():
                     help="NL-Poisson CG: 0 plain (the reference's), 1 Jacobi-preconditioned "
                          "(default: the library's, 0)")
     ap.add_argument("--pm-bound", type=int, default=None, choices=[0, 1, 2],
-                    help="PatchMatch lower bound: 2 patch means and deviations, 1 means, 0 every candidate "
-                         "evaluated (default: the library's, 2)")
+                    help="PatchMatch lower bound: 1 patch means, 2 means and deviations, 0 every candidate "
+                         "evaluated (default: the library's, 1)")
     ap.add_argument("--pm-tile", type=int, default=None,
                     help="PatchMatch work distribution: 0 static block ranges, n > 0 a device work queue of n "
                          "target points per grab (default: the library's, 1)")
-    ap.add_argument("--pm-check", type=int, default=None,
-                    help="PatchMatch early-termination rows of 9x9 kernels, bit r = test after row r "
-                         "(default: the library's, one test after 4 rows)")
     ap.add_argument("--graph-loop", type=int, default=None, choices=[0, 1, 2],
                     help="iteration loops as CUDA graphs: 1 plain runs and lockstep batches, 2 also worker "
                          "batches, 0 host loops (for profilers that cannot see into conditional graphs); "

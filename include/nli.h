@@ -448,11 +448,13 @@ int nli_ctx_set_batch_width(nli_ctx *ctx, int width);
  *                                  differences, weighted by the patch
  *                                  weights) differ from the target's by
  *                                  enough that its distance provably cannot
- *                                  beat the current match: 2 (default) by
- *                                  the weighted means and standard
- *                                  deviations (L2 kinds; L1 uses the means),
- *                                  1 by the means alone (Jensen's
- *                                  inequality), 0 every candidate is
+ *                                  beat the current match: 1 (default) by
+ *                                  the weighted means (Jensen's
+ *                                  inequality); 2 by the means and the
+ *                                  weighted standard deviations (L2 kinds;
+ *                                  L1 uses the means): fewer candidates
+ *                                  evaluated, but slower on the 512x512
+ *                                  benchmark; 0 every candidate is
  *                                  evaluated.  The bound keeps a rounding
  *                                  margin, so fields and distances are
  *                                  identical in all three.
@@ -471,13 +473,6 @@ int nli_ctx_set_batch_width(nli_ctx *ctx, int width);
  *                                  grab (1..1024, default 1); 0 static
  *                                  ranges (block b takes the b-th contiguous
  *                                  range).  Identical fields.
- *   NLI_TUNE_PM_CHECK              PatchMatch kernels of compiled patch
- *                                  sizes (9x9): bit r set = after window row
- *                                  r, a step of candidates stops when every
- *                                  partial sum has reached the current
- *                                  distance (exact: the terms are
- *                                  non-negative); 0 (default) one test after
- *                                  rows / 2 - 1 rows.  Identical fields.
  * nli_ctx_get_tuning reads them back. */
 #define NLI_TUNE_CG_CLUSTER_CAP 0
 #define NLI_TUNE_CG_UNKNOWNS_PER_CTA 1
@@ -490,7 +485,6 @@ int nli_ctx_set_batch_width(nli_ctx *ctx, int width);
 #define NLI_TUNE_PM_BOUND 8
 #define NLI_TUNE_BATCH_GROUPS 9
 #define NLI_TUNE_PM_TILE 10
-#define NLI_TUNE_PM_CHECK 11
 int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value);
 int nli_ctx_get_tuning(nli_ctx *ctx, int knob, int *value);
 /* The seed image `index` of a batch runs with. */

@@ -491,7 +491,7 @@ class Context:
         return outs, [s.as_dict() for s in st]
 
     TUNE_CG_CLUSTER_CAP, TUNE_CG_UNKNOWNS_PER_CTA, TUNE_BATCH_WIDTH, TUNE_PM_VARIANT, TUNE_CG_PRECOND, TUNE_GRAPH_LOOP = 0, 1, 2, 3, 4, 5
-    TUNE_CG_SINGLE_MAX, TUNE_BATCH_MODE, TUNE_PM_BOUND, TUNE_BATCH_GROUPS, TUNE_PM_TILE, TUNE_PM_CHECK = 6, 7, 8, 9, 10, 11
+    TUNE_CG_SINGLE_MAX, TUNE_BATCH_MODE, TUNE_PM_BOUND, TUNE_BATCH_GROUPS, TUNE_PM_TILE = 6, 7, 8, 9, 10
 
     def set_tuning(self, knob, value):
         self._check(self.lib.nli_ctx_set_tuning(self.h, knob, value))

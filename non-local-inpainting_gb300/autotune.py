@@ -3,9 +3,8 @@ thread-block clusters of the NL-Poisson conjugate gradient (CTAs per
 cluster, unknowns per CTA), the largest CG system one CTA solves alone
 (NLI_TUNE_CG_SINGLE_MAX), the way the 9x9 PatchMatch kernels read their
 windows (NLI_TUNE_PM_VARIANT), the PatchMatch lower-bound test
-(NLI_TUNE_PM_BOUND), work distribution (NLI_TUNE_PM_TILE: static ranges
-or a device work queue, and its tile) and early-termination rows
-(NLI_TUNE_PM_CHECK), how a batch runs (NLI_TUNE_BATCH_MODE, the worker
+(NLI_TUNE_PM_BOUND) and work distribution (NLI_TUNE_PM_TILE: static ranges
+or a device work queue, and its tile), how a batch runs (NLI_TUNE_BATCH_MODE, the worker
 contexts' width, the lockstep sub-groups NLI_TUNE_BATCH_GROUPS).  Each
 candidate is timed with CUDA events on a representative case on the
 context's own device; the fastest is set on the context
@@ -212,37 +211,6 @@ def tune_pm_tile(ctx, case=None, tiles=(0, 4, 16, 64), repeats=3, seed=0):
     return {"best": choice, "ms": times}
 
 
-def _time_patchmatch(ctx, case, knob, values, repeats, seed):
-    import torch
-    dist, pm, u, src, tgt = case if case is not None else patchmatch_case(ctx)
-    times = {}
-    for v in values:
-        ctx.set_tuning(knob, v)
-        ctx.set_seed(seed)
-        ctx.patchmatch(dist, pm, u, src, u, tgt, want_energy=False)  # warm
-        best = float("inf")
-        for _ in range(repeats):
-            ctx.set_seed(seed)
-            torch.cuda.synchronize()
-            a, b = _events(torch)
-            a.record()
-            ctx.patchmatch(dist, pm, u, src, u, tgt, want_energy=False)
-            b.record()
-            torch.cuda.synchronize()
-            best = min(best, a.elapsed_time(b))
-        times[v] = best
-    choice = min(times, key=times.get)
-    ctx.set_tuning(knob, choice)
-    return {"best": choice, "ms": times}
-
-
-def tune_pm_check(ctx, case=None, masks=(0, 1 << 4, 1 << 5, 1 << 6, (1 << 3) | (1 << 6)), repeats=3, seed=0):
-    """Times one PatchMatch call per set of early-termination rows (bit r:
-    test after window row r; 0 the library's default) and keeps the
-    fastest.  Returns {"best": mask, "ms": {mask: ms}}."""
-    return _time_patchmatch(ctx, case, ctx.TUNE_PM_CHECK, masks, repeats, seed)
-
-
 def _time_batch(ctx, items, params):
     import torch
     torch.cuda.synchronize()
@@ -292,12 +260,11 @@ def device_key(device=0):
     return "%s|%d SMs|sm_%d%d" % (pr.name, pr.multi_processor_count, pr.major, pr.minor)
 
 
-_SCALARS = ("batch_width", "pm_variant", "cg_single", "pm_bound", "batch_mode", "batch_groups", "pm_tile",
-            "pm_check")
+_SCALARS = ("batch_width", "pm_variant", "cg_single", "pm_bound", "batch_mode", "batch_groups", "pm_tile")
 
 
 def save(path, key, cg=None, batch_width=None, pm_variant=None, cg_single=None, pm_bound=None, batch_mode=None,
-         batch_groups=None, pm_tile=None, pm_check=None):
+         batch_groups=None, pm_tile=None):
     """Stores the choices for one device key in a JSON cache file (other
     devices' entries are kept)."""
     import json
@@ -310,7 +277,7 @@ def save(path, key, cg=None, batch_width=None, pm_variant=None, cg_single=None, 
     if cg is not None:
         entry["cg"] = [int(cg[0]), int(cg[1])]
     values = dict(batch_width=batch_width, pm_variant=pm_variant, cg_single=cg_single, pm_bound=pm_bound,
-                  batch_mode=batch_mode, batch_groups=batch_groups, pm_tile=pm_tile, pm_check=pm_check)
+                  batch_mode=batch_mode, batch_groups=batch_groups, pm_tile=pm_tile)
     for name in _SCALARS:
         if values[name] is not None:
             entry[name] = int(values[name])
@@ -337,15 +304,14 @@ def load(ctx, path, key):
 
 
 def apply(ctx, cg=None, batch_width=None, pm_variant=None, cg_single=None, pm_bound=None, batch_mode=None,
-          batch_groups=None, pm_tile=None, pm_check=None):
+          batch_groups=None, pm_tile=None):
     """Re-applies stored choices: cg = (cap, unknowns per CTA)."""
     if cg is not None:
         ctx.set_tuning(ctx.TUNE_CG_CLUSTER_CAP, int(cg[0]))
         ctx.set_tuning(ctx.TUNE_CG_UNKNOWNS_PER_CTA, int(cg[1]))
     for knob, value in ((ctx.TUNE_PM_VARIANT, pm_variant), (ctx.TUNE_CG_SINGLE_MAX, cg_single),
                         (ctx.TUNE_PM_BOUND, pm_bound), (ctx.TUNE_BATCH_MODE, batch_mode),
-                        (ctx.TUNE_BATCH_GROUPS, batch_groups), (ctx.TUNE_PM_TILE, pm_tile),
-                        (ctx.TUNE_PM_CHECK, pm_check)):
+                        (ctx.TUNE_BATCH_GROUPS, batch_groups), (ctx.TUNE_PM_TILE, pm_tile)):
         if value is not None:
             ctx.set_tuning(knob, int(value))
     if batch_width is not None:

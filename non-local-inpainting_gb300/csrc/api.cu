@@ -666,10 +666,6 @@ int nli_ctx_set_tuning(nli_ctx *ctx, int knob, int value)
 		if (value < 0 || value > 1024) return NLI_E_INVALID;
 		ctx->tune_pm_tile = value;
 		return NLI_OK;
-	case NLI_TUNE_PM_CHECK:
-		if (value < 0 || value >= (1 << 16)) return NLI_E_INVALID;
-		ctx->tune_pm_check = value;
-		return NLI_OK;
 	}
 	return NLI_E_INVALID;
 }
@@ -689,7 +685,6 @@ int nli_ctx_get_tuning(nli_ctx *ctx, int knob, int *value)
 	case NLI_TUNE_PM_BOUND: *value = ctx->tune_pm_bound; return NLI_OK;
 	case NLI_TUNE_BATCH_GROUPS: *value = ctx->tune_batch_groups; return NLI_OK;
 	case NLI_TUNE_PM_TILE: *value = ctx->tune_pm_tile; return NLI_OK;
-	case NLI_TUNE_PM_CHECK: *value = ctx->tune_pm_check; return NLI_OK;
 	}
 	return NLI_E_INVALID;
 }

@@ -134,10 +134,9 @@ struct nli_ctx {
 	                                     // 1 in nli_process only, 2 also in batches, 0 never
 	int tune_cg_single_max = 1024;       // CG systems of at most this many unknowns: one CTA
 	int tune_batch_mode = 1;             // batches: 1 lockstep (process.cu), 0 worker contexts (batch.cu)
-	int tune_pm_bound = 2;               // PatchMatch lower bound: 0 off, 1 patch means, 2 means and deviations
+	int tune_pm_bound = 1;               // PatchMatch lower bound: 0 off, 1 patch means, 2 means and deviations
 	int tune_batch_groups = 4;           // lockstep: concurrent sub-groups per launch-sharing group
 	int tune_pm_tile = 1;                // PatchMatch: 0 static ranges, n > 0 work queue of n points per grab
-	int tune_pm_check = 0;               // PatchMatch: rows (bit mask) after which to test early termination; 0 default
 	bool batch_worker = false;           // a worker context of nli_process_batch
 	int max_smem_optin = 0;              // dynamic shared memory per block at most
 	std::vector<nli_ctx *> workers;
@@ -187,7 +186,6 @@ struct nli_ctx {
 		tune_cg_single_max = o.tune_cg_single_max;
 		tune_pm_bound = o.tune_pm_bound;
 		tune_pm_tile = o.tune_pm_tile;
-		tune_pm_check = o.tune_pm_check;
 	}
 
 	template <class T>

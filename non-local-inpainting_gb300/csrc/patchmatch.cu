@@ -146,9 +146,6 @@ struct PmArgs {
 	// 1: the tables also hold the weighted standard deviations (of the
 	// image and of its forward differences), and the bound uses them
 	int dev;
-	// compiled patch sizes: bit r set = the early-termination test runs
-	// after window row r
-	unsigned check_rows;
 	// device work queue (null: static ranges): the call's counters, one
 	// per launch (init, then each sweep), zeroed before the init launch;
 	// a warp takes `tile` consecutive target points per grab
@@ -664,13 +661,18 @@ __device__ __forceinline__ void eval_candidates(const PmArgs &p, const float *s_
 			return __all_sync(kFull, !active || c != 0 || part >= bound);
 		};
 		if constexpr (P > 0) {
-			// a test after each row r with bit r of check_rows set (by
-			// default after the first (P + G) / 2 - 1 rows: 4 of 10 for 9x9
-			// L2 combined)
+			// one test after the first (P + G) / 2 - 1 rows (4 of 10 for 9x9
+			// L2 combined).  On the 512x512 benchmark without the lower bound
+			// it stops 57.5 % of the candidates and is 1.6 % faster than a
+			// test at half the window (65 % stopped); two tests (rows 5 and 7,
+			// or 3 and 5 and 7) cost more than they save.  With the bound,
+			// tests after rows 5, 6 or 7, or after 4 and 7, take the same
+			// time within 0.3 %
+			constexpr int kCheckRow = (P + G) / 2 - 2;
 #pragma unroll
 			for (int r = 0; r < P + G; r++) {
 				row(r);
-				if (((p.check_rows >> r) & 1u) && check()) {
+				if (r == kCheckRow && check()) {
 					stop = true;
 					break;
 				}
@@ -1359,16 +1361,6 @@ static void run_batch_kernels(nli_ctx *ctx, const DistArgs &a, const PmBatchArgs
 	}
 }
 
-// Rows after which the compiled-size kernels test for early termination
-// (NLI_TUNE_PM_CHECK): the context's mask, or by default one test after the
-// first rows / 2 - 1 rows (4 of 10 for 9x9 L2 combined, the fastest single
-// row on the 512x512 benchmark without the lower bound).
-static unsigned pm_check_rows(const nli_ctx *ctx, int rows)
-{
-	if (ctx->tune_pm_check) return (unsigned)ctx->tune_pm_check;
-	return 1u << std::max(rows / 2 - 2, 0);
-}
-
 void patchmatch_batch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patchmatch_params &pm, int C, int n,
                           const PmBatchItem *items, const int *active)
 {
@@ -1412,7 +1404,6 @@ void patchmatch_batch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli
 		p.vmax = it.mom ? it.vmax : nullptr;
 		// the item's table holds room for the deviations (4 tables)
 		p.dev = (it.mom && ctx->tune_pm_bound == 2 && dp.kind != NLI_DIST_L1_NORM) ? 1 : 0;
-		p.check_rows = pm_check_rows(ctx, p.rows);
 		p.queue = nullptr;  // the launch's queue is B.queue
 		p.tile = 0;
 		T.flag = it.flag;
@@ -1577,7 +1568,6 @@ void patchmatch_run(nli_ctx *ctx, const nli_distance_params &dp, const nli_patch
 		p.tmom = tmom;
 		p.vmax = vmax;
 		p.dev = smom ? dev : 0;
-		p.check_rows = pm_check_rows(ctx, p.rows);
 		p.queue = nullptr;
 		p.tile = ctx->tune_pm_tile;
 		if (p.tile > 0) {

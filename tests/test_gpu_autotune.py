@@ -76,7 +76,7 @@ def test_tune_cg_single_and_pm_bound(gpu_ctx):
     res = autotune.tune_pm_bound(gpu_ctx, case, repeats=1)
     assert sorted(res["ms"]) == [0, 1, 2]
     assert gpu_ctx.get_tuning(gpu_ctx.TUNE_PM_BOUND) == res["best"]
-    autotune.apply(gpu_ctx, cg_single=1024, pm_bound=2)
+    autotune.apply(gpu_ctx, cg_single=1024, pm_bound=1)
 
 
 def test_tune_batch_mode_and_groups(gpu_ctx):

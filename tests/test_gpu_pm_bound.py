@@ -1,6 +1,6 @@
 """The lower bounds of PatchMatch (NLI_TUNE_PM_BOUND): a candidate whose
-weighted patch means (1), or means and standard deviations (2, the
-default), differ enough from the target's is not evaluated, because it
+weighted patch means (1, the default), or means and standard deviations
+(2), differ enough from the target's is not evaluated, because it
 provably cannot beat the current match.  The bounds keep a rounding
 margin, so the fields and distances must be bit for bit those of
 evaluating every candidate -- for every distance kind and channel count,
@@ -46,7 +46,7 @@ def both(ctx, fn):
             r = fn()
             out.append((r, ctx.counters()["candidates"] - c0))
         finally:
-            ctx.set_tuning(ctx.TUNE_PM_BOUND, 2)
+            ctx.set_tuning(ctx.TUNE_PM_BOUND, 1)
     return out
 
 

@@ -110,29 +110,3 @@ def test_tile_knob_validates(gpu_ctx):
     gpu_ctx.set_tuning(gpu_ctx.TUNE_PM_TILE, 1024)
     assert gpu_ctx.get_tuning(gpu_ctx.TUNE_PM_TILE) == 1024
     gpu_ctx.set_tuning(gpu_ctx.TUNE_PM_TILE, 1)
-
-
-@pytest.mark.parametrize("mask", [1 << 2, 1 << 6, (1 << 3) | (1 << 6), 0x3FF])
-def test_check_rows_keep_fields(gpu_ctx, mask):
-    """Where the early-termination test runs (NLI_TUNE_PM_CHECK) changes
-    only how many candidates stop early, never the field: the test is
-    exact because every term is non-negative."""
-    img, mask_img = scene(5, 140, 120, 16)
-    d = _abi.DistanceParams(_abi.NLI_DIST_L2_COMBINED, 9, 9, 10000.0, 0.05, 0.4)
-    pm = _abi.PatchMatchParams(7, 30, -1)
-    ext = npy(gpu_ctx.extended_domain(mask_img, 9, 9))
-    s, t, _ = gpu_ctx.scale_masks(ext, 4, True)
-
-    def one():
-        gpu_ctx.set_seed(31)
-        nnf, dist, e = gpu_ctx.patchmatch(d, pm, img, s, img, t)
-        return npy(nnf), npy(dist), e
-
-    want = one()
-    gpu_ctx.set_tuning(gpu_ctx.TUNE_PM_CHECK, mask)
-    try:
-        got = one()
-    finally:
-        gpu_ctx.set_tuning(gpu_ctx.TUNE_PM_CHECK, 0)
-    for a, b in zip(got, want):
-        assert np.array_equal(np.asarray(a), np.asarray(b))

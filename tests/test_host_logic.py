@@ -19,7 +19,7 @@ class FakeCtx:
         import nli_gb300 as pkg
         for k in ("TUNE_CG_CLUSTER_CAP", "TUNE_CG_UNKNOWNS_PER_CTA", "TUNE_BATCH_WIDTH", "TUNE_PM_VARIANT",
                   "TUNE_CG_PRECOND", "TUNE_GRAPH_LOOP", "TUNE_CG_SINGLE_MAX", "TUNE_BATCH_MODE", "TUNE_PM_BOUND",
-                  "TUNE_BATCH_GROUPS", "TUNE_PM_TILE", "TUNE_PM_CHECK"):
+                  "TUNE_BATCH_GROUPS", "TUNE_PM_TILE"):
             setattr(self, k, getattr(pkg.Context, k))
         self.tuning = {}
         self.batch_width = None
@@ -52,13 +52,13 @@ def test_cache_round_trip_every_knob(tmp_path):
     path = str(tmp_path / "tuning.json")
     ctx = FakeCtx()
     autotune.save(path, "dev", cg=(8, 1024), batch_width=4, pm_variant=1, cg_single=2048, pm_bound=0,
-                  batch_mode=1, batch_groups=4, pm_tile=16, pm_check=72)
+                  batch_mode=1, batch_groups=4, pm_tile=16)
     got = autotune.load(ctx, path, "dev")
     assert got == {"cg": [8, 1024], "batch_width": 4, "pm_variant": 1, "cg_single": 2048, "pm_bound": 0,
-                   "batch_mode": 1, "batch_groups": 4, "pm_tile": 16, "pm_check": 72}
+                   "batch_mode": 1, "batch_groups": 4, "pm_tile": 16}
     assert ctx.tuning == {ctx.TUNE_CG_CLUSTER_CAP: 8, ctx.TUNE_CG_UNKNOWNS_PER_CTA: 1024, ctx.TUNE_PM_VARIANT: 1,
                           ctx.TUNE_CG_SINGLE_MAX: 2048, ctx.TUNE_PM_BOUND: 0, ctx.TUNE_BATCH_MODE: 1,
-                          ctx.TUNE_BATCH_GROUPS: 4, ctx.TUNE_PM_TILE: 16, ctx.TUNE_PM_CHECK: 72}
+                          ctx.TUNE_BATCH_GROUPS: 4, ctx.TUNE_PM_TILE: 16}
     assert ctx.batch_width == 4
 
 
@@ -68,7 +68,7 @@ def test_tuning_constants_match_the_header():
     here = os.path.dirname(os.path.abspath(__file__))
     header = open(os.path.join(here, "..", "include", "nli.h")).read()
     defines = dict((m.group(1), int(m.group(2))) for m in re.finditer(r"#define NLI_(TUNE_\w+) (\d+)", header))
-    assert len(defines) == 12
+    assert len(defines) == 11
     for name, value in defines.items():
         assert getattr(pkg.Context, name) == value, name
 
