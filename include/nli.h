@@ -425,12 +425,14 @@ int nli_ctx_set_batch_width(nli_ctx *ctx, int width);
  *                                  remaining PatchMatch / update iterations
  *                                  as one CUDA graph whose while node tests
  *                                  the stopping rule on the device (no host
- *                                  round trip per iteration); batches keep
+ *                                  round trip per iteration), and lockstep
+ *                                  batches run each pyramid rank's loop as
+ *                                  one graph; worker-context batches keep
  *                                  the host loop, where other images' work
  *                                  hides the round trips.  2: the graph in
- *                                  batches too.  0: the host loop everywhere.
- *                                  Identical results; the graph is not used
- *                                  while profiling is on.
+ *                                  worker-context batches too.  0: the host
+ *                                  loop everywhere.  Identical results; the
+ *                                  graph is not used while profiling is on.
  *   NLI_TUNE_CG_SINGLE_MAX         CG systems (per channel) of at most this
  *                                  many unknowns are solved by one CTA with
  *                                  block barriers only, instead of a cluster
