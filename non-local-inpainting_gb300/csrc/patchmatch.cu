@@ -1334,7 +1334,9 @@ static void run_batch_kernels(nli_ctx *ctx, const DistArgs &a, const PmBatchArgs
 	// dynamic shared memory up to the opt-in limit less the kernels' static
 	// shared memory (the work-list prefix), raised once per device
 	static std::atomic<uint32_t> raised{0};  // one bit per device
-	static int dyn_max[32];
+	// written by whichever thread raises the limit first (concurrent
+	// sub-groups may race to it with the same value)
+	static std::atomic<int> dyn_max[32];
 	const uint32_t bit = 1u << (ctx->device & 31);
 	if (!(raised.load(std::memory_order_acquire) & bit)) {
 		cudaFuncAttributes fa_init, fa_sweep;
@@ -1343,10 +1345,11 @@ static void run_batch_kernels(nli_ctx *ctx, const DistArgs &a, const PmBatchArgs
 		const int dmax = ctx->max_smem_optin - (int)std::max(fa_init.sharedSizeBytes, fa_sweep.sharedSizeBytes);
 		NLI_CUDA(cudaFuncSetAttribute(k_pm_init_batch<KIND, C, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmax));
 		NLI_CUDA(cudaFuncSetAttribute(k_pm_sweep_batch<KIND, C, P>, cudaFuncAttributeMaxDynamicSharedMemorySize, dmax));
-		dyn_max[ctx->device & 31] = dmax;
+		dyn_max[ctx->device & 31].store(dmax, std::memory_order_relaxed);
 		raised.fetch_or(bit, std::memory_order_release);
 	}
-	NLI_REQUIRE(smem <= (size_t)dyn_max[ctx->device & 31], NLI_E_UNSUPPORTED, "PatchMatch shared memory too large");
+	NLI_REQUIRE(smem <= (size_t)dyn_max[ctx->device & 31].load(std::memory_order_relaxed), NLI_E_UNSUPPORTED,
+	            "PatchMatch shared memory too large");
 	const int block = pm_threads(kPmShared);
 	const int grid = ctx->num_sms;
 	{
