@@ -84,3 +84,36 @@ def test_bench_workloads_and_throughput():
             bench.WORKLOAD = "nlpoisson512"
     # whole-job throughput: N ranks x steps x Mpix per rank and step / seconds
     assert bench.job_throughput(2, 5, 0.262144, 1000.0) == pytest.approx(2 * 5 * 0.262144)
+
+
+def test_formula_candidates():
+    """The reference's candidate count per process(): per scale, calls
+    (iterations plus one per transition the scale takes part in) x N_t x
+    (1 + I (2 + floor(log2 max(W, H)) + 1))."""
+    st = {"scales": 3, "width": [512, 256, 128], "height": [400, 200, 100], "targets": [1000, 300, 50],
+          "iterations": [5, 7, 9]}
+    want = (5 + 1) * 1000 * (1 + 10 * (2 + 10)) + (7 + 2) * 300 * (1 + 10 * (2 + 9)) + \
+        (9 + 1) * 50 * (1 + 10 * (2 + 8))
+    assert bench.formula_candidates(st, 10) == want
+    st1 = {"scales": 1, "width": [64], "height": [64], "targets": [20], "iterations": [3]}
+    assert bench.formula_candidates(st1, 4) == 3 * 20 * (1 + 4 * (2 + 7))
+
+
+def test_batch_reference_gaps_only_compare_the_same_batch(tmp_path, monkeypatch):
+    """References are compared only with the batch they were made from
+    (seed, count, largest side): another batch's item i is another image."""
+    import numpy as np
+    rng = np.random.default_rng(0)
+    img = rng.uniform(0, 255, (20, 30, 3)).astype(np.float32)
+    mask = np.zeros((20, 30), np.uint8)
+    mask[5:10, 5:12] = 1
+    ref_hole = img[mask > 0] + 2.0
+    np.savez(tmp_path / "batch_reference_01.npz", hole=ref_hole, index=1, batch=np.array([5, 64, 1024]))
+    monkeypatch.setattr(bench, "GOLDEN", str(tmp_path))
+    out = img.copy()
+    out[mask > 0] += 1.0  # closer to the truth than the reference
+    items = [(img, mask, "nlmeans", 2)] * 2
+    rows = bench.batch_reference_gaps(items, [img, out], (5, 64, 1024))
+    assert len(rows) == 1 and rows[0]["index"] == 1
+    assert rows[0]["gap_db"] == pytest.approx(20 * np.log10(2.0), rel=1e-6)
+    assert bench.batch_reference_gaps(items, [img, out], (5, 32, 768)) == []
